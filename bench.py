@@ -1,0 +1,331 @@
+"""Benchmark: progressive path tracing throughput (Mrays/s) on GB300.
+
+One step = one pass of the wavefront path tracer over one frame: 1 sample per
+pixel of the material-sweep workload (8x8 icosphere grid, 327,684 triangles,
+1920x1080, max depth 12, point light + quad emitter), i.e. one call of the
+reference's per-frame launch. Ray count = extension rays + shadow rays
+actually traced.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the oracle
+integrator, FP32, all host threads) on a bounded band of rows of the same
+frame, because the reference's own OptiX path does not build here.
+Multi-GPU (torchrun): every rank renders its own replica of the frame (the
+work is independent per pixel and sample, so there is no data-path
+collective); value = rays of all ranks / slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "material sweep: 8x8 icospheres (subdiv 4) + ground, 327,684 tris, point light + quad emitter",
+            "scene": "spheres", "width": 1920, "height": 1080, "max_depth": 12, "spp_per_step": 1}
+METRIC = "Mrays/s (extension + shadow rays traced), progressive path tracing, 1 spp per step"
+NODE_BYTES = 64      # one BVH2 node: two child boxes + refs
+TRI_BYTES = 48       # one leaf-ordered triangle record (3 x float4)
+RAY_IO_BYTES = 48    # ray in (origin, dir, tmax, path id) + hit out (t, u, v, id)
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/optpt_clocks.csv"
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_render_band(scene, rows, threads, spp=1, sample_base=1000):
+    """Times the oracle integrator (FP32, `threads` host threads) on a band of
+    rows of the workload frame. Returns (seconds, rays, pixel samples)."""
+    from oracle import oracle as orc
+    a = scene.arrays()
+    w, h = WORKLOAD["width"], WORKLOAD["height"]
+    U, V, W = _camera_basis(a["camEye"], a["camTarget"], a["camUp"], a["camFovYDeg"], w / h)
+    cam = list(a["camEye"]) + U + V + W + list(a["bgColour"])
+    view = orc.SceneView(scene.struct, 4)
+    y0 = (h - rows) // 2
+    t0 = time.perf_counter()
+    _, _, cnt = view.render(cam, w, h, 1, sample_base, spp, WORKLOAD["max_depth"], y0=y0, y1=y0 + rows,
+                            precision=32, threads=threads)
+    dt = time.perf_counter() - t0
+    return dt, int(cnt[0] + cnt[1]), rows * w * spp
+
+
+def _camera_basis(eye, target, up, fov, aspect):
+    """Camera::setupUvwCoordinatSystem (src/camera.cpp:19-40)."""
+    e, t, u = (np.array(v, np.float64) for v in (eye, target, up))
+    W = t - e
+    W /= np.linalg.norm(W)
+    u /= np.linalg.norm(u)
+    U = np.cross(u, -W)
+    U /= np.linalg.norm(U)
+    V = np.cross(-W, U)
+    V /= np.linalg.norm(V)
+    vl = np.tan(0.5 * np.radians(fov))
+    return list((U * vl * aspect).astype(np.float32)), list((V * vl).astype(np.float32)), list(W.astype(np.float32))
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the oracle integrator on the host cores."""
+    if rank != 0:
+        return
+    import optix_pt_gb300 as opt
+    scene = opt.Scene.procedural(WORKLOAD["scene"])
+    threads = os.cpu_count()
+    rows = args.cpu_rows
+    for _ in range(args.warmup):
+        cpu_render_band(scene, max(1, rows // 8), threads)
+    tot_t, tot_rays, tot_samples = 0.0, 0, 0
+    for k in range(args.steps):
+        dt, rays, samples = cpu_render_band(scene, rows, threads, sample_base=2000 + k)
+        tot_t += dt
+        tot_rays += rays
+        tot_samples += samples
+    value = tot_rays / tot_t / 1e6
+    sample = "%d rows x 1920 px x 1 spp per step (of 1080 rows), depth 12" % rows
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene)", "config": dict(WORKLOAD, parallelism="host threads"),
+            "samples_per_s": tot_samples / tot_t,
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    import optix_pt_gb300 as opt
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    scene = opt.Scene.procedural(WORKLOAD["scene"])
+    r = opt.Renderer(scene)
+    w, h = WORKLOAD["width"], WORKLOAD["height"]
+    r.setupOutputBuffer(w, h)
+    a = scene.arrays()
+    r.setupCamera(a["camEye"], a["camTarget"], a["camUp"], a["camFovYDeg"])
+    r.set_max_depth(WORKLOAD["max_depth"])
+    lp = r.launch_params()
+    lp.seed = 1 + rank
+    r.updateLaunchParams(lp)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            r.render(1, stream)
+        torch.cuda.synchronize()
+        st0 = r.stats()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local_rank) as clk:
+            for k in range(args.steps):
+                flush.zero_()                       # L2 flushed between timed steps (not timed)
+                starts[k].record(stream)
+                r.render(1, stream)
+                ends[k].record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+        st1 = r.stats()
+    rays = (st1["extensionRays"] - st0["extensionRays"]) + (st1["shadowRays"] - st0["shadowRays"])
+    samples = st1["pathSamples"] - st0["pathSamples"]
+    t = torch.tensor([ms, float(rays), float(samples)], dtype=torch.float64, device=dev)
+    if world > 1:
+        tmax = t.clone()
+        dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:3], op=dist.ReduceOp.SUM)
+        t[0] = tmax[0]
+    ms_all, rays_all, samples_all = t.tolist()
+    value = rays_all / (ms_all / 1e3) / 1e6
+
+    # End to end through the public API with host buffers: per step the frame
+    # constants go host -> device (80 B) and the tone-mapped frame buffer
+    # (float4 per pixel) comes back into pinned host memory.
+    host_fb = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
+    barrier()
+    torch.cuda.synchronize()
+    st0 = r.stats()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        lp = r.launch_params()
+        r.updateLaunchParams(lp)
+        r.render(1, stream)
+        opt.check(opt.lib.optpt_read_frame_buffer(r._h, host_fb.data_ptr(), stream.cuda_stream))
+    e2e_s = time.perf_counter() - t0
+    st1 = r.stats()
+    e2e_rays = (st1["extensionRays"] - st0["extensionRays"]) + (st1["shadowRays"] - st0["shadowRays"])
+    e = torch.tensor([e2e_s, float(e2e_rays)], dtype=torch.float64, device=dev)
+    if world > 1:
+        emax = e.clone()
+        dist.all_reduce(emax[0:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(e[1:2], op=dist.ReduceOp.SUM)
+        e[0] = emax[0]
+    e2e_value = e[1].item() / e[0].item() / 1e6
+
+    if rank != 0:
+        r.close()
+        return
+
+    # Roofline of the dominant kernel: per-kernel CUDA-event times of a
+    # profiled pass and the exact BVH work per ray of the same frame.
+    prof = r.profile(2, stream)
+    cnt = r.traversal_counts(1, stream)
+    kms = prof["ms"]
+    dominant = max(kms, key=kms.get)
+    ext_rays = max(1, cnt["extensionRays"])
+    sh_rays = max(1, cnt["shadowRays"])
+    nodes_ext, tris_ext = cnt["extensionNodes"] / ext_rays, cnt["extensionTris"] / ext_rays
+    nodes_sh, tris_sh = cnt["shadowNodes"] / sh_rays, cnt["shadowTris"] / sh_rays
+    bytes_ext = RAY_IO_BYTES + nodes_ext * NODE_BYTES + tris_ext * TRI_BYTES
+    bytes_sh = RAY_IO_BYTES + 4 + nodes_sh * NODE_BYTES + tris_sh * TRI_BYTES
+    per_kernel_bytes = {
+        "extend": bytes_ext * prof["extensionRays"],
+        "shadow": bytes_sh * prof["shadowRays"],
+        "shade": 256.0 * prof["extensionRays"],
+        "accumulate": 64.0 * 2 * w * h,
+        "generate": 64.0 * 2 * w * h,
+    }
+    peak, peak_kind = _peaks()
+    achieved = per_kernel_bytes[dominant] / (kms[dominant] / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "extend_traffic.json")
+    if dominant == "extend" and os.path.exists(tp):
+        traffic = json.load(open(tp)).get("bytes_per_launch_scaled")
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "bytes_per_ray": {"extension": bytes_ext, "shadow": bytes_sh},
+                "bvh_work_per_ray": {"ext_nodes": nodes_ext, "ext_tris": tris_ext, "sh_nodes": nodes_sh,
+                                     "sh_tris": tris_sh},
+                "kernel_ms_per_pass": {k: v / 2 for k, v in kms.items()},
+                "kernel_share": {k: v / sum(kms.values()) for k, v in kms.items()}}
+
+    # CPU baseline: the oracle integrator on this host's cores, bounded band.
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        threads = os.cpu_count()
+        dt, crays, csamples = cpu_render_band(scene, args.cpu_rows, threads)
+        cpu = {"value": crays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "%d rows x 1920 px x 1 spp of the same frame, FP32 oracle integrator, %.1f s" % (
+                   args.cpu_rows, dt)}
+
+    passes_launches = 3 + 4 * WORKLOAD["max_depth"]
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_all / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene, no glTF assets)",
+            "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single GPU",
+                           l2="flushed between timed steps (256 MB write, outside the events)"),
+            "samples_per_s": samples_all / (ms_all / 1e3),
+            "rays_per_step": rays_all / args.steps / world,
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": 80,
+                    "d2h_bytes_per_step": w * h * 16},
+            "gpu_launches": passes_launches * args.steps,
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
+    print(json.dumps(line))
+    r.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=48)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    import __graft_entry__
+    __graft_entry__.build()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

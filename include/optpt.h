@@ -1,0 +1,271 @@
+/* optpt: C ABI of the GB300 progressive path tracer.
+ *
+ * This is the drop-in boundary for markcmagro/optix_pt's render call. The
+ * reference drives rendering through the C++ class Renderer
+ * (include/renderer.h:19-206): an init sequence that loads the scene and builds
+ * the acceleration structure, then per frame updateLaunchParams() + launch(),
+ * then getFrameBuffer(). Each entry point below names the reference member or
+ * program it replaces. The C++ Renderer in include/optix_pt/renderer.hpp keeps
+ * the reference's method names on top of these calls.
+ *
+ * Conventions: every function returns an int status (OPTPT_OK or a negative
+ * OPTPT_ERR_* code), never throws and never traps; optpt_last_error() gives a
+ * message for the last failure on the calling thread. Pointers documented as
+ * "device" are CUDA device pointers; "stream" is a cudaStream_t passed as
+ * void* (NULL = legacy default stream). One renderer handle must not be used
+ * by two host threads at once.
+ */
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+#include "optix_pt/launch_params.h"
+#include "optix_pt/light.h"
+#include "optix_pt/material_data.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OPTPT_OK 0
+#define OPTPT_ERR_INVALID (-1)   /* bad argument or size                    */
+#define OPTPT_ERR_CUDA (-2)      /* CUDA runtime or kernel launch failure   */
+#define OPTPT_ERR_IO (-3)        /* file missing or unreadable              */
+#define OPTPT_ERR_PARSE (-4)     /* malformed JSON scene description        */
+#define OPTPT_ERR_NOMEM (-5)     /* host or device allocation failed        */
+#define OPTPT_ERR_TIMEOUT (-6)   /* a bounded device wait gave up           */
+#define OPTPT_ERR_STATE (-7)     /* call out of order (e.g. no framebuffer) */
+
+typedef struct optpt_renderer optpt_renderer;
+
+/* Message for the last failing call on this thread ("" if none). */
+const char *optpt_last_error(void);
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int optpt_version(void);
+
+/* ------------------------------------------------------------------ scene */
+
+/* An RGBA8 texture image. wrap: 0 repeat, 1 clamp, 2 mirror. srgb: decode
+ * the colour channels from sRGB (reference: src/renderer.cpp:1471-1483). */
+typedef struct optpt_texture {
+    uint32_t width;
+    uint32_t height;
+    const uint8_t *rgba;
+    int32_t wrapS;
+    int32_t wrapT;
+    int32_t srgb;
+    int32_t pad;
+} optpt_texture;
+
+/* A flattened, world-space triangle scene plus camera and frame settings:
+ * what the reference's glTF loader produces (SceneProperties,
+ * include/scene_properties.h:11) and SceneDesc adds (include/scene_desc.h:9-39).
+ * All arrays are host memory owned by the caller. */
+typedef struct optpt_scene {
+    const float *positions;     /* float3 per vertex                          */
+    uint32_t numVertices;
+    const float *normals;       /* float3 per vertex, or NULL                 */
+    const float *texCoords;     /* float2 per vertex, or NULL                 */
+    const int32_t *triIndices;  /* int3 per triangle                          */
+    uint32_t numTriangles;
+    const int32_t *matIndices;  /* material per triangle                      */
+    const MaterialData *materials;
+    uint32_t numMaterials;
+    const Light *lights;
+    uint32_t numLights;
+    const optpt_texture *textures;
+    uint32_t numTextures;
+    float camEye[3];
+    float camTarget[3];
+    float camUp[3];
+    float camFovYDeg;
+    uint32_t resX;
+    uint32_t resY;
+    float bgColour[3];
+    uint32_t spp;               /* samples per pixel the workload asks for    */
+    uint32_t maxDepth;
+} optpt_scene;
+
+/* Builds one of the seeded procedural scenes into library-owned host arrays
+ * (released with optpt_scene_release): "cornell" (36 triangles),
+ * "spheres" (8x8 icosphere material sweep, 327,682 triangles).
+ * Stands in for the reference's glTF import (src/gltf_loader.cpp:72). */
+int optpt_scene_procedural(const char *name, uint32_t seed, optpt_scene *out);
+void optpt_scene_release(optpt_scene *scene);
+
+/* Resolves a scene-selection list in the reference's configs/*.json format
+ * (src/scene_desc.cpp:118-153: {"scene": id, id: name}) and parses the named
+ * scene file (src/scene_desc.cpp:50-116). A scene file names either
+ * "gltf scene file" (not supported: returns OPTPT_ERR_INVALID) or
+ * "procedural scene"; "renderer.dimensions" and "renderer.background colour"
+ * override the scene's defaults. */
+int optpt_scene_from_config(const char *sceneListPath, optpt_scene *out);
+
+/* ------------------------------------------------------------------ renderer */
+
+typedef struct optpt_options {
+    uint32_t sppBatch;   /* samples traced side by side in one wavefront (0 = auto) */
+    uint32_t blockSize;  /* threads per block for the wavefront kernels (0 = auto)  */
+    uint32_t leafSize;   /* maximum triangles per BVH leaf, 1..8 (0 = auto)          */
+    uint32_t useGraph;   /* capture the bounce loop in a CUDA graph (default 1)      */
+} optpt_options;
+
+/* Uploads the scene and builds the BVH on the GPU. Replaces the reference's
+ * init sequence Renderer(SceneDesc&) .. loadScene() .. buildAccel(true)
+ * (src/renderer.cpp:24,191,267; OptiX context/module/pipeline/SBT set-up has
+ * no counterpart). Also performs setupOutputBuffer(resX, resY) and
+ * setupCamera() from the scene's camera. `options` may be NULL. */
+int optpt_create(const optpt_scene *scene, const optpt_options *options, optpt_renderer **out);
+int optpt_destroy(optpt_renderer *r); /* Renderer::~Renderer (src/renderer.cpp:79) */
+
+/* Renderer::setupOutputBuffer (src/renderer.cpp:839): (re)allocates the
+ * frame buffers and clears the accumulation. */
+int optpt_setup_output_buffer(optpt_renderer *r, uint32_t width, uint32_t height);
+
+/* Renderer::setupCamera + Camera::setupUvwCoordinatSystem
+ * (src/renderer.cpp:861, src/camera.cpp:19-40). */
+int optpt_setup_camera(optpt_renderer *r, const float eye[3], const float target[3], const float up[3],
+                       float fovYDeg);
+
+/* Renderer::setupLaunchParams / updateLaunchParams (src/renderer.cpp:882,910):
+ * get returns the current frame contract; set applies sample, seed, eye/U/V/W,
+ * vis, tone mapping, gamma, maxDepth and bgColour (buffer pointers, sizes and
+ * handles are owned by the renderer and ignored). */
+int optpt_get_launch_params(const optpt_renderer *r, LaunchParams *out);
+int optpt_set_launch_params(optpt_renderer *r, const LaunchParams *lp);
+
+/* Renders `spp` more samples per pixel into the FP64 accumulation and
+ * rewrites frameBuffer / accumFrameBuffer, asynchronously on `stream`.
+ * Replaces optixLaunch of __raygen__renderFrame (src/renderer.cpp:943,
+ * cu/device_programs.cu:15-106): the reference launches 1 spp per call. */
+int optpt_render(optpt_renderer *r, uint32_t spp, void *stream);
+
+/* Renderer::launch (src/renderer.cpp:940-958): 1 spp, wait, copy the
+ * tone-mapped frame buffer to the renderer's host buffer. */
+int optpt_launch(optpt_renderer *r);
+
+/* Renderer::getFrameBuffer (src/renderer.cpp:1344): host float4 w*h owned
+ * by the renderer, valid after optpt_launch. NULL before. */
+const float *optpt_get_frame_buffer(optpt_renderer *r);
+
+/* Renderer::getSampleCount / resetSampleCount (src/renderer.cpp:1349-1357);
+ * reset also clears the accumulation. */
+uint32_t optpt_get_sample_count(const optpt_renderer *r);
+int optpt_reset_sample_count(optpt_renderer *r);
+
+/* Device pointers of the output buffers (valid until the next
+ * optpt_setup_output_buffer): float4 frameBuffer and accumFrameBuffer, and
+ * the FP64 per-pixel sums (double4 sum, double4 sum of squares; xyz used). */
+int optpt_device_buffers(optpt_renderer *r, float **frameBuffer, float **accumFrameBuffer, double **sum,
+                         double **sumSq);
+
+/* Copies the tone-mapped frame buffer (float4 w*h) to caller host memory,
+ * ordered on `stream`, and waits for it. */
+int optpt_read_frame_buffer(optpt_renderer *r, float *rgbaHost, void *stream);
+
+/* Copies the FP64 per-pixel sums (double4 sum and sum of squares, xyz used,
+ * w*h each) to caller host memory, ordered on `stream`, and waits for it. */
+int optpt_read_accum(optpt_renderer *r, double *sumHost, double *sumSqHost, void *stream);
+
+/* Counters accumulated since creation (read after the GPU work finished). */
+typedef struct optpt_stats {
+    uint64_t extensionRays;  /* rays traced by the closest-hit kernel   */
+    uint64_t shadowRays;     /* rays traced by the occlusion kernel     */
+    uint64_t pathSamples;    /* pixel samples completed                 */
+    uint64_t nanSamples;     /* samples dropped for NaN radiance        */
+    uint32_t bvhNodes;       /* BVH2 nodes in use                       */
+    uint32_t bvhLeaves;
+    uint32_t sppBatch;
+    uint32_t blockSize;
+} optpt_stats;
+int optpt_get_stats(optpt_renderer *r, optpt_stats *out);
+
+/* Per-kernel device time (ms) of one extra render of `spp` samples, launched
+ * without a graph with CUDA events around each kernel on `stream`. Index:
+ * 0 generate, 1 extend (closest hit), 2 shade, 3 shadow (occlusion),
+ * 4 accumulate + tone map. Also returns the rays each kernel class traced. */
+typedef struct optpt_kernel_times {
+    double ms[5];
+    uint64_t launches[5];
+    uint64_t extensionRays;
+    uint64_t shadowRays;
+} optpt_kernel_times;
+int optpt_render_profiled(optpt_renderer *r, uint32_t spp, void *stream, optpt_kernel_times *out);
+
+/* BVH work of one extra render of `spp` samples, run with counting variants
+ * of the traversal kernels (slower; not for timing): rays traced, BVH nodes
+ * visited and triangles tested, for extension and shadow rays. Feeds the
+ * bytes-per-ray model of the traversal roofline. */
+typedef struct optpt_traversal_work {
+    uint64_t extensionRays;
+    uint64_t extensionNodes;
+    uint64_t extensionTris;
+    uint64_t shadowRays;
+    uint64_t shadowNodes;
+    uint64_t shadowTris;
+} optpt_traversal_work;
+int optpt_traversal_counts(optpt_renderer *r, uint32_t spp, void *stream, optpt_traversal_work *out);
+
+/* ------------------------------------------------------------------ parity entry points */
+
+/* Closest-hit (anyHit = 0) or occlusion (anyHit = 1) queries against the
+ * renderer's BVH, replacing optixTrace (cu/device_programs.cu:63,
+ * cu/path_tracer.cu:396,485). Device arrays: rays = 2 float4 per ray
+ * (origin.xyz, tmin; direction.xyz, tmax); hits = 1 float4 per ray
+ * (t, u, v, primitive index as int bits; -1 = miss). Ties in t resolve to the
+ * smaller primitive index. The pixel/sample/depth needed by alpha-blend
+ * materials are taken as 0. */
+int optpt_trace(optpt_renderer *r, const float *rays, float *hits, uint32_t n, int anyHit, void *stream);
+
+/* The sorted 30-bit Morton codes and the primitive order of the BVH leaves
+ * (host copies of numTriangles entries each), and the leaf size used. */
+int optpt_bvh_leaf_order(optpt_renderer *r, uint32_t *mortonSorted, int32_t *primOrder);
+
+/* BVH2 topology in host memory: per node (child0, child1, count0, count1),
+ * where count > 0 marks a leaf covering primOrder[child .. child+count). */
+int optpt_bvh_nodes(optpt_renderer *r, int32_t *nodes4, uint32_t capacity, uint32_t *numNodes);
+
+/* One BSDF query per element, evaluated by the device BSDF code. Device
+ * arrays of optpt_bsdf_query / optpt_bsdf_result (layouts below). The query
+ * procedure is the closest-hit program's: categoriseMaterial, the
+ * MaterialMetallicRoughness set-up, metallicRoughnessBrdf(l = wi, v = wo),
+ * then metallicRoughnessSample with pdf *= categoryWeight
+ * (cu/path_tracer.cu:231-370,400,524-526); uniforms are consumed from xs in
+ * the reference's draw order. */
+typedef struct optpt_bsdf_query {
+    float baseColour[3];
+    float emission[3];
+    float sheenColour[3];
+    float metallic;
+    float roughness;
+    float specular;
+    float transmissionWeight;
+    float subsurfaceWeight;
+    float coatWeight;
+    float coatRoughness;
+    float sheenRoughnessMat;
+    float sheenRoughness;
+    float ior;
+    uint32_t category;
+    float n[3];
+    float wo[3];
+    float wi[3];
+    float xs[12];
+} optpt_bsdf_query;
+
+typedef struct optpt_bsdf_result {
+    uint32_t category;
+    int32_t ret;
+    int32_t used;
+    float categoryWeight;
+    float f[3];
+    float dir[3];
+    float bsdf[3];
+    float pdf;
+} optpt_bsdf_result;
+
+int optpt_bsdf_batch(const optpt_bsdf_query *queries, optpt_bsdf_result *results, uint32_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,293 @@
+"""optix_pt_gb300: GB300-native progressive path tracer behind optix_pt's render surface.
+
+Python mirror of the reference's host interface (class Renderer,
+include/renderer.h:19-206, and SceneDesc, include/scene_desc.h:9-39) over the
+C ABI in include/optpt.h. The reference's method names are kept
+(setupOutputBuffer, setupCamera, updateLaunchParams, launch, getFrameBuffer,
+getSampleCount, resetSampleCount, set/getVis, set/getToneMapping*,
+set/getGammaCorrection*); OptiX set-up steps that have no counterpart are
+accepted as no-ops so a caller's init sequence runs unchanged.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import BSDF_QUERY, BSDF_RESULT, OptptError, check, lib
+
+__all__ = ["Scene", "SceneDesc", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
+           "library_path"]
+
+library_path = _ffi.LIB_PATH
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)  # torch.cuda.Stream
+
+
+class Scene:
+    """A flattened triangle scene (the reference's SceneProperties + SceneDesc)."""
+
+    def __init__(self, struct, owned):
+        self._s = struct
+        self._owned = owned
+
+    @classmethod
+    def procedural(cls, name, seed=1):
+        s = _ffi.SceneStruct()
+        check(lib.optpt_scene_procedural(name.encode(), seed, ctypes.byref(s)))
+        return cls(s, True)
+
+    @classmethod
+    def from_config(cls, scene_list_path):
+        s = _ffi.SceneStruct()
+        check(lib.optpt_scene_from_config(str(scene_list_path).encode(), ctypes.byref(s)))
+        return cls(s, True)
+
+    def __del__(self):
+        if getattr(self, "_owned", False):
+            lib.optpt_scene_release(ctypes.byref(self._s))
+            self._owned = False
+
+    @property
+    def struct(self):
+        return self._s
+
+    @property
+    def num_triangles(self):
+        return self._s.numTriangles
+
+    def _arr(self, ptr, n, width, dtype):
+        if not ptr or n == 0:
+            return None
+        return np.ctypeslib.as_array(ptr, shape=(n * width,)).astype(dtype).reshape(n, width) if width > 1 else \
+            np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype)
+
+    def arrays(self):
+        """Copies of the scene arrays as numpy (for the oracle and tests)."""
+        s = self._s
+        out = {
+            "positions": self._arr(s.positions, s.numVertices, 3, np.float32),
+            "normals": self._arr(s.normals, s.numVertices, 3, np.float32),
+            "texCoords": self._arr(s.texCoords, s.numVertices, 2, np.float32),
+            "triIndices": self._arr(s.triIndices, s.numTriangles, 3, np.int32),
+            "matIndices": self._arr(s.matIndices, s.numTriangles, 1, np.int32),
+            "materials": bytes(ctypes.string_at(s.materials, ctypes.sizeof(_ffi.MaterialData) * s.numMaterials)),
+            "numMaterials": s.numMaterials,
+            "lights": bytes(ctypes.string_at(s.lights, ctypes.sizeof(_ffi.Light) * s.numLights))
+            if s.numLights else b"",
+            "numLights": s.numLights,
+            "camEye": list(s.camEye), "camTarget": list(s.camTarget), "camUp": list(s.camUp),
+            "camFovYDeg": s.camFovYDeg, "resX": s.resX, "resY": s.resY, "bgColour": list(s.bgColour),
+            "spp": s.spp, "maxDepth": s.maxDepth,
+        }
+        return out
+
+
+SceneDesc = Scene.from_config  # the reference constructs SceneDesc from the scene list
+
+
+class Renderer:
+    """The reference's Renderer (include/renderer.h:19-206) on the GB300 engine."""
+
+    def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True):
+        self.scene = scene
+        opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0)
+        h = ctypes.c_void_p()
+        check(lib.optpt_create(ctypes.byref(scene.struct), ctypes.byref(opt), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.optpt_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    # ---- init sequence of the reference (src/main_window.cpp:36-49) ----
+    def initOptix(self):
+        pass
+
+    def createContext(self):
+        pass
+
+    def loadScene(self):
+        pass
+
+    def buildAccel(self, build=True):
+        pass
+
+    def setupCompilationOptions(self):
+        pass
+
+    def createModules(self):
+        pass
+
+    def createProgramGroups(self):
+        pass
+
+    def createPipeline(self):
+        pass
+
+    def setupSbt(self):
+        pass
+
+    def createDenoiser(self):
+        pass
+
+    def createRandomState(self):
+        pass
+
+    def setupLaunchParams(self, scene_desc=None):
+        pass
+
+    def setupOutputBuffer(self, width, height):
+        check(lib.optpt_setup_output_buffer(self._h, width, height))
+
+    def setupCamera(self, eye, target, up, fov_y_deg):
+        check(lib.optpt_setup_camera(self._h, _ffi.f3(*eye), _ffi.f3(*target), _ffi.f3(*up), fov_y_deg))
+
+    # ---- per frame ----
+    def launch_params(self):
+        lp = _ffi.LaunchParams()
+        check(lib.optpt_get_launch_params(self._h, ctypes.byref(lp)))
+        return lp
+
+    def updateLaunchParams(self, lp=None):
+        if lp is not None:
+            check(lib.optpt_set_launch_params(self._h, ctypes.byref(lp)))
+
+    def _set(self, **kw):
+        lp = self.launch_params()
+        for k, v in kw.items():
+            setattr(lp, k, v)
+        check(lib.optpt_set_launch_params(self._h, ctypes.byref(lp)))
+
+    def launch(self):
+        """1 sample per pixel, wait, copy the frame buffer to host (src/renderer.cpp:940-958)."""
+        check(lib.optpt_launch(self._h))
+
+    def getFrameBuffer(self):
+        p = lib.optpt_get_frame_buffer(self._h)
+        if not p:
+            return None
+        lp = self.launch_params()
+        return np.ctypeslib.as_array(p, shape=(lp.h, lp.w, 4)).copy()
+
+    def getSampleCount(self):
+        return lib.optpt_get_sample_count(self._h)
+
+    def resetSampleCount(self):
+        check(lib.optpt_reset_sample_count(self._h))
+
+    def setVis(self, vis):
+        self._set(vis=vis)
+
+    def getVis(self):
+        return self.launch_params().vis
+
+    def setToneMappingState(self, enable):
+        self._set(toneMapping=1 if enable else 0)
+
+    def getToneMappingState(self):
+        return bool(self.launch_params().toneMapping)
+
+    def setToneMappingImpl(self, impl):
+        self._set(toneMappingImpl=impl)
+
+    def getToneMappingImpl(self):
+        return self.launch_params().toneMappingImpl
+
+    def setGammaCorrectionState(self, enable):
+        self._set(gammaCorrection=1 if enable else 0)
+
+    def getGammaCorrectionState(self):
+        return self.launch_params().gammaCorrection
+
+    def setGammaCorrectionTerm(self, value):
+        self._set(gammaTerm=value)
+
+    def getGammaCorrectionTerm(self):
+        return self.launch_params().gammaTerm
+
+    def getDenoiserState(self):
+        return False
+
+    def setDenoiserState(self, on):
+        if on:
+            raise OptptError(-1, "the OptiX denoiser is not part of this renderer")
+
+    # ---- extensions ----
+    def set_max_depth(self, depth):
+        self._set(maxDepth=depth)
+
+    def set_seed(self, seed):
+        self._set(seed=seed)
+
+    def render(self, spp, stream=None):
+        check(lib.optpt_render(self._h, spp, _stream_handle(stream)))
+
+    def frame_buffer(self, stream=None):
+        lp = self.launch_params()
+        out = np.empty((lp.h, lp.w, 4), np.float32)
+        check(lib.optpt_read_frame_buffer(self._h, out.ctypes.data, _stream_handle(stream)))
+        return out
+
+    def accum(self, stream=None):
+        """FP64 per-pixel (sum, sum of squares, samples): arrays (h, w, 3)."""
+        lp = self.launch_params()
+        s = np.empty((lp.h, lp.w, 4), np.float64)
+        q = np.empty((lp.h, lp.w, 4), np.float64)
+        check(lib.optpt_read_accum(self._h, s.ctypes.data, q.ctypes.data, _stream_handle(stream)))
+        return s[..., :3], q[..., :3], self.getSampleCount()
+
+    def device_buffers(self):
+        fb, afb, s, q = (ctypes.c_void_p() for _ in range(4))
+        check(lib.optpt_device_buffers(self._h, ctypes.byref(fb), ctypes.byref(afb), ctypes.byref(s),
+                                       ctypes.byref(q)))
+        return fb.value, afb.value, s.value, q.value
+
+    def stats(self):
+        st = _ffi.Stats()
+        check(lib.optpt_get_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _ffi.Stats._fields_}
+
+    def profile(self, spp, stream=None):
+        kt = _ffi.KernelTimes()
+        check(lib.optpt_render_profiled(self._h, spp, _stream_handle(stream), ctypes.byref(kt)))
+        names = ["generate", "extend", "shade", "shadow", "accumulate"]
+        return {"ms": dict(zip(names, list(kt.ms))), "launches": dict(zip(names, list(kt.launches))),
+                "extensionRays": kt.extensionRays, "shadowRays": kt.shadowRays}
+
+    def traversal_counts(self, spp, stream=None):
+        c = _ffi.TraversalCounts()
+        check(lib.optpt_traversal_counts(self._h, spp, _stream_handle(stream), ctypes.byref(c)))
+        return {k: getattr(c, k) for k, _ in _ffi.TraversalCounts._fields_}
+
+    def trace(self, rays_ptr, hits_ptr, n, any_hit=False, stream=None):
+        """Device pointers: rays (2 x float4 per ray), hits (float4 per ray)."""
+        check(lib.optpt_trace(self._h, rays_ptr, hits_ptr, n, 1 if any_hit else 0, _stream_handle(stream)))
+
+    def bvh_leaf_order(self):
+        n = self.scene.num_triangles
+        codes = np.zeros(n, np.uint32)
+        order = np.zeros(n, np.int32)
+        check(lib.optpt_bvh_leaf_order(self._h, codes.ctypes.data, order.ctypes.data))
+        return codes, order
+
+    def bvh_nodes(self):
+        cnt = ctypes.c_uint32()
+        check(lib.optpt_bvh_nodes(self._h, None, 0, ctypes.byref(cnt)))
+        nodes = np.zeros((max(cnt.value, 1), 4), np.int32)
+        check(lib.optpt_bvh_nodes(self._h, nodes.ctypes.data, cnt.value, ctypes.byref(cnt)))
+        return nodes[:cnt.value]
+
+
+def bsdf_batch(queries_ptr, results_ptr, n, stream=None):
+    """Device BSDF queries (optpt_bsdf_query -> optpt_bsdf_result), device pointers."""
+    check(lib.optpt_bsdf_batch(queries_ptr, results_ptr, n, _stream_handle(stream)))

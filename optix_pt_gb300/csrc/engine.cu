@@ -1,0 +1,938 @@
+// The renderer behind the C ABI (include/optpt.h): scene upload, GPU BVH
+// build, wavefront buffers, the CUDA-graph-captured bounce loop, and the
+// parity entry points. Replaces the reference's Renderer
+// (src/renderer.cpp:24-1762) minus OptiX set-up, denoiser and GL display.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+#include "../../include/optpt.h"
+#include "engine.h"
+
+int uploadSrgbTable();
+
+namespace {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string &msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+int cudaFail(cudaError_t e, const char *where)
+{
+    return fail(OPTPT_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_OR_RETURN(expr, where)                                                                                    \
+    do {                                                                                                               \
+        cudaError_t e_ = (expr);                                                                                       \
+        if (e_ != cudaSuccess)                                                                                         \
+            return cudaFail(e_, where);                                                                                \
+    } while (0)
+
+template <class T> cudaError_t upload(T *&dst, const T *src, size_t count)
+{
+    dst = nullptr;
+    if (count == 0 || src == nullptr)
+        return cudaSuccess;
+    cudaError_t e = cudaMalloc((void **)&dst, sizeof(T) * count);
+    if (e != cudaSuccess)
+        return e;
+    return cudaMemcpy(dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+}
+
+float3 f3(const float *p) { return make_float3(p[0], p[1], p[2]); }
+
+}  // namespace
+
+struct optpt_renderer {
+    // scene (device)
+    float *dPositions = nullptr, *dNormals = nullptr, *dTexCoords = nullptr;
+    int *dTriIndices = nullptr, *dMatIndices = nullptr;
+    uint32_t *dTriFlags = nullptr;
+    DevMaterial *dMaterials = nullptr;
+    DevLight *dLights = nullptr;
+    Light *dLightsPublic = nullptr;
+    float4 *dEmisV = nullptr, *dEmisRad = nullptr;
+    float2 *dEmisTc = nullptr;
+    uint32_t *dTexels = nullptr;
+    int4 *dTexInfo = nullptr;
+    BvhBuild bvh{};
+    DevScene scene{};
+    int numTris = 0, numEmissive = 0, numLights = 0;
+
+    // frame
+    LaunchParams lp{};
+    optpt_options opt{};
+    uint32_t w = 0, h = 0, sppBatch = 1;
+    WaveBufs q{};
+    AccumBufs acc{};
+    uint32_t *dState = nullptr;
+    LaunchShape shape{};
+    std::vector<float> hostFb;
+    bool hostFbValid = false;
+
+    // graph of one pass, re-captured when the frame parameters change
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    bool graphDirty = true;
+    cudaStream_t ownStream = nullptr;
+
+    FrameConst *dFrameConst = nullptr;
+
+    FrameParams frameParams() const
+    {
+        FrameParams fp{};
+        fp.w = w;
+        fp.h = h;
+        fp.npix = w * h;
+        fp.sppBatch = sppBatch;
+        fp.numPaths = w * h * sppBatch;
+        fp.maxDepth = lp.maxDepth;
+        fp.state = dState;
+        fp.fc = dFrameConst;
+        return fp;
+    }
+
+    FrameConst frameConst() const
+    {
+        auto bits = [](uint32_t u) {
+            float f;
+            memcpy(&f, &u, 4);
+            return f;
+        };
+        FrameConst c;
+        c.eye = make_float4(lp.eye[0], lp.eye[1], lp.eye[2], bits(lp.seed));
+        c.U = make_float4(lp.U[0], lp.U[1], lp.U[2], bits((uint32_t)lp.vis));
+        const uint32_t tone = (lp.toneMapping ? 1u : 0u) | (lp.toneMappingImpl ? 2u : 0u) | (lp.gammaCorrection ? 4u : 0u);
+        c.V = make_float4(lp.V[0], lp.V[1], lp.V[2], bits(tone));
+        c.W = make_float4(lp.W[0], lp.W[1], lp.W[2], lp.gammaTerm);
+        c.bg = make_float4(lp.bgColour[0], lp.bgColour[1], lp.bgColour[2], 0.0f);
+        return c;
+    }
+
+    void freeFrame()
+    {
+        if (graphExec)
+            cudaGraphExecDestroy(graphExec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        graphExec = nullptr;
+        graph = nullptr;
+        graphDirty = true;
+        cudaFree(q.pathT);
+        cudaFree(q.pathL);
+        for (int k = 0; k < 2; ++k) {
+            cudaFree(q.rayO[k]);
+            cudaFree(q.rayD[k]);
+            cudaFree(q.shO[k]);
+            cudaFree(q.shD[k]);
+            cudaFree(q.shC[k]);
+        }
+        cudaFree(q.hit);
+        cudaFree(acc.sum);
+        cudaFree(acc.sumSq);
+        cudaFree(acc.frameBuffer);
+        cudaFree(acc.accumFrameBuffer);
+        unsigned long long *totals = q.totals;
+        uint32_t *counters = q.counters;
+        q = WaveBufs{};
+        q.totals = totals;
+        q.counters = counters;
+        acc = AccumBufs{};
+    }
+
+    ~optpt_renderer()
+    {
+        freeFrame();
+        cudaFree(q.totals);
+        cudaFree(q.counters);
+        cudaFree(dState);
+        cudaFree(dFrameConst);
+        freeBvh(bvh);
+        cudaFree(dPositions);
+        cudaFree(dNormals);
+        cudaFree(dTexCoords);
+        cudaFree(dTriIndices);
+        cudaFree(dMatIndices);
+        cudaFree(dTriFlags);
+        cudaFree(dMaterials);
+        cudaFree(dLights);
+        cudaFree(dLightsPublic);
+        cudaFree(dEmisV);
+        cudaFree(dEmisRad);
+        cudaFree(dEmisTc);
+        cudaFree(dTexels);
+        cudaFree(dTexInfo);
+        if (ownStream)
+            cudaStreamDestroy(ownStream);
+    }
+};
+
+namespace {
+
+// Camera::setParams + setupUvwCoordinatSystem (src/camera.cpp:6-40).
+void cameraBasis(const float eye[3], const float target[3], const float up[3], float fovYDeg, float aspect,
+                 float U[3], float V[3], float W[3])
+{
+    auto nrm = [](double v[3]) {
+        double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        v[0] /= l;
+        v[1] /= l;
+        v[2] /= l;
+    };
+    auto crs = [](const double a[3], const double b[3], double o[3]) {
+        o[0] = a[1] * b[2] - a[2] * b[1];
+        o[1] = a[2] * b[0] - a[0] * b[2];
+        o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    double w[3] = {(double)target[0] - eye[0], (double)target[1] - eye[1], (double)target[2] - eye[2]};
+    nrm(w);
+    double upn[3] = {up[0], up[1], up[2]};
+    nrm(upn);
+    double mw[3] = {-w[0], -w[1], -w[2]}, u[3], v[3];
+    crs(upn, mw, u);
+    nrm(u);
+    crs(mw, u, v);
+    nrm(v);
+    const double vLen = std::tan(0.5 * fovYDeg * 3.14159265358979323846 / 180.0);
+    const double uLen = vLen * aspect;
+    for (int k = 0; k < 3; ++k) {
+        U[k] = (float)(u[k] * uLen);
+        V[k] = (float)(v[k] * vLen);
+        W[k] = (float)w[k];
+    }
+}
+
+int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
+{
+    r->freeFrame();
+    r->w = width;
+    r->h = height;
+    const size_t npix = (size_t)width * height;
+    uint32_t b = r->opt.sppBatch;
+    if (b == 0) {
+        b = (uint32_t)((1u << 21) / (npix ? npix : 1));
+        b = b < 1 ? 1 : (b > 64 ? 64 : b);
+    }
+    r->sppBatch = b;
+    const size_t P = npix * b;
+    auto al = [&](float4 *&p, size_t n) { return cudaMalloc((void **)&p, sizeof(float4) * (n ? n : 1)); };
+    CUDA_OR_RETURN(al(r->q.pathT, P), "alloc pathT");
+    CUDA_OR_RETURN(al(r->q.pathL, P), "alloc pathL");
+    for (int k = 0; k < 2; ++k) {
+        CUDA_OR_RETURN(al(r->q.rayO[k], P), "alloc rays");
+        CUDA_OR_RETURN(al(r->q.rayD[k], P), "alloc rays");
+        CUDA_OR_RETURN(al(r->q.shO[k], P), "alloc shadow rays");
+        CUDA_OR_RETURN(al(r->q.shD[k], P), "alloc shadow rays");
+        CUDA_OR_RETURN(al(r->q.shC[k], P), "alloc shadow rays");
+    }
+    CUDA_OR_RETURN(al(r->q.hit, P), "alloc hits");
+    CUDA_OR_RETURN(cudaMalloc((void **)&r->acc.sum, sizeof(Acc4) * (npix ? npix : 1)), "alloc accum");
+    CUDA_OR_RETURN(cudaMalloc((void **)&r->acc.sumSq, sizeof(Acc4) * (npix ? npix : 1)), "alloc accum");
+    CUDA_OR_RETURN(al(r->acc.frameBuffer, npix), "alloc frameBuffer");
+    CUDA_OR_RETURN(al(r->acc.accumFrameBuffer, npix), "alloc accumFrameBuffer");
+    CUDA_OR_RETURN(cudaMemset(r->acc.sum, 0, sizeof(Acc4) * npix), "clear accum");
+    CUDA_OR_RETURN(cudaMemset(r->acc.sumSq, 0, sizeof(Acc4) * npix), "clear accum");
+    CUDA_OR_RETURN(cudaMemset(r->acc.frameBuffer, 0, sizeof(float4) * npix), "clear fb");
+    CUDA_OR_RETURN(cudaMemset(r->acc.accumFrameBuffer, 0, sizeof(float4) * npix), "clear fb");
+    CUDA_OR_RETURN(cudaMemset(r->dState, 0, sizeof(uint32_t) * 4), "clear state");
+    r->lp.sample = 0;
+    r->lp.w = width;
+    r->lp.h = height;
+    r->lp.frameBuffer = (float *)r->acc.frameBuffer;
+    r->lp.accumFrameBuffer = (float *)r->acc.accumFrameBuffer;
+    r->hostFb.assign(npix * 4, 0.0f);
+    r->hostFbValid = false;
+    const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 256;
+    r->shape.block = blk;
+    r->shape.gridGenerate = occupancyGrid(0, blk);
+    r->shape.gridExtend = occupancyGrid(1, blk);
+    r->shape.gridShade = occupancyGrid(2, blk);
+    r->shape.gridShadow = occupancyGrid(3, blk);
+    r->shape.gridAccum = occupancyGrid(4, blk);
+    r->graphDirty = true;
+    return OPTPT_OK;
+}
+
+// One pass: sppBatch samples for every pixel.
+void enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaEvent_t *ev, int *kind,
+                 bool count = false)
+{
+    int e = 0;
+    auto mark = [&](int k) {
+        if (ev) {
+            cudaEventRecord(ev[e], st);
+            kind[e] = k;
+            ++e;
+        }
+    };
+    cudaMemsetAsync(r->q.counters, 0, sizeof(uint32_t) * CNT_TOTAL, st);
+    mark(0);
+    launchGenerate(r->shape, fp, r->q, st);
+    for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
+        mark(1);
+        launchExtend(r->shape, r->scene, fp, r->q, (int)d, st, count);
+        mark(2);
+        launchShade(r->shape, r->scene, fp, r->q, (int)d, st);
+        mark(3);
+        launchShadow(r->shape, r->scene, fp, r->q, (int)d, 0, st, count);
+        launchShadow(r->shape, r->scene, fp, r->q, (int)d, 1, st, count);
+    }
+    mark(4);
+    launchAccumulate(r->shape, fp, r->q, r->acc, st);
+    launchAdvance(fp, r->dState, st);
+    mark(5);
+}
+
+int ensureGraph(optpt_renderer *r, cudaStream_t st)
+{
+    if (!r->graphDirty && r->graphExec)
+        return OPTPT_OK;
+    if (r->graphExec)
+        cudaGraphExecDestroy(r->graphExec);
+    if (r->graph)
+        cudaGraphDestroy(r->graph);
+    r->graphExec = nullptr;
+    r->graph = nullptr;
+    const FrameParams fp = r->frameParams();
+    CUDA_OR_RETURN(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    enqueuePass(r, fp, st, nullptr, nullptr);
+    cudaError_t e = cudaStreamEndCapture(st, &r->graph);
+    if (e != cudaSuccess)
+        return cudaFail(e, "end capture");
+    CUDA_OR_RETURN(cudaGraphInstantiate(&r->graphExec, r->graph, 0), "instantiate graph");
+    r->graphDirty = false;
+    return OPTPT_OK;
+}
+
+bool validScene(const optpt_scene *s, std::string &why)
+{
+    if (!s) {
+        why = "scene is NULL";
+        return false;
+    }
+    if (s->numTriangles && (!s->positions || !s->triIndices || !s->matIndices)) {
+        why = "positions, triIndices and matIndices are required";
+        return false;
+    }
+    if (s->numMaterials == 0 || !s->materials) {
+        why = "at least one material is required";
+        return false;
+    }
+    for (uint32_t t = 0; t < s->numTriangles; ++t) {
+        for (int k = 0; k < 3; ++k) {
+            int v = s->triIndices[3 * t + k];
+            if (v < 0 || (uint32_t)v >= s->numVertices) {
+                why = "triangle " + std::to_string(t) + " has a vertex index out of range";
+                return false;
+            }
+        }
+        int m = s->matIndices[t];
+        if (m < 0 || (uint32_t)m >= s->numMaterials) {
+            why = "triangle " + std::to_string(t) + " has a material index out of range";
+            return false;
+        }
+    }
+    for (uint32_t m = 0; m < s->numMaterials; ++m) {
+        const int32_t *tex = &s->materials[m].baseColourTexture;
+        for (int k = 0; k < 6; ++k) {
+            if (tex[k] >= (int32_t)s->numTextures) {
+                why = "material " + std::to_string(m) + " names a texture out of range";
+                return false;
+            }
+        }
+    }
+    for (uint32_t t = 0; t < s->numTextures; ++t) {
+        if (!s->textures[t].rgba || s->textures[t].width == 0 || s->textures[t].height == 0) {
+            why = "texture " + std::to_string(t) + " is empty";
+            return false;
+        }
+    }
+    if (s->maxDepth > OPT_MAX_DEPTH) {
+        why = "maxDepth above " + std::to_string(OPT_MAX_DEPTH);
+        return false;
+    }
+    return true;
+}
+
+DevMaterial toDev(const MaterialData &m, uint32_t numTextures)
+{
+    DevMaterial d{};
+    d.baseColour = make_float4(m.baseColour[0], m.baseColour[1], m.baseColour[2], m.baseColour[3]);
+    d.emissionCutoff = make_float4(m.emission[0], m.emission[1], m.emission[2], m.alphaCutoff);
+    d.sheen = make_float4(m.sheenColour[0], m.sheenColour[1], m.sheenColour[2], m.sheenRoughness);
+    d.p0 = make_float4(m.ior, m.roughness, m.metallic, m.specular);
+    d.p1 = make_float4(m.transmissionWeight, m.subsurfaceWeight, m.coatWeight, m.coatRoughness);
+    const int32_t tex[6] = {m.baseColourTexture, m.normalTexture, m.metallicRoughnessTexture, m.emissiveTexture,
+                            m.sheenColourTexture, m.sheenRoughnessTexture};
+    const uint8_t has[6] = {m.hasBaseColourTexture, m.hasNormalTexture, m.hasMetallicRoughnessTexture,
+                            m.hasEmissiveTexture, m.hasSheenColourTexture, m.hasSheenRoughnessTexture};
+    const TextureTransform *tf[6] = {&m.baseColourTexTf, &m.normalTexTf, &m.metallicRoughnessTexTf,
+                                     &m.emissiveTexTf, &m.sheenColourTexTf, &m.sheenRoughnessTexTf};
+    int mask = 0;
+    for (int k = 0; k < 6; ++k) {
+        if (has[k] && tex[k] >= 0 && (uint32_t)tex[k] < numTextures)
+            mask |= 1 << k;
+        d.tf[k] = make_float4(tf[k]->offset[0], tf[k]->offset[1], tf[k]->scale[0], tf[k]->scale[1]);
+    }
+    d.flags = make_int4((int)m.category, m.alphaMode, mask, 0);
+    d.tex0 = make_int4(tex[0], tex[1], tex[2], tex[3]);
+    d.tex1 = make_int4(tex[4], tex[5], 0, 0);
+    return d;
+}
+
+DevLight toDev(const Light &l)
+{
+    DevLight d{};
+    int type = l.type;
+    float tf;
+    memcpy(&tf, &type, 4);
+    d.p0Type = make_float4(l.p0[0], l.p0[1], l.p0[2], tf);
+    d.radianceDist = make_float4(l.radiance[0], l.radiance[1], l.radiance[2], l.distance);
+    d.normalCosW = make_float4(l.normal[0], l.normal[1], l.normal[2], l.cosWidth);
+    d.cosFalloff = make_float4(l.cosFalloffStart, 0.0f, 0.0f, 0.0f);
+    return d;
+}
+
+int checkRenderable(optpt_renderer *r)
+{
+    if (!r)
+        return fail(OPTPT_ERR_INVALID, "renderer is NULL");
+    if (r->w == 0 || r->h == 0)
+        return fail(OPTPT_ERR_STATE, "no output buffer (call optpt_setup_output_buffer)");
+    return OPTPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *optpt_last_error(void) { return g_lastError.c_str(); }
+
+int optpt_internal_set_error(int code, const char *msg)
+{
+    g_lastError = msg ? msg : "";
+    return code;
+}
+
+int optpt_version(void) { return 100; }
+
+int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_renderer **out)
+{
+    if (!out)
+        return fail(OPTPT_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    if (!validScene(s, why))
+        return fail(OPTPT_ERR_INVALID, why);
+    optpt_renderer *r = new (std::nothrow) optpt_renderer();
+    if (!r)
+        return fail(OPTPT_ERR_NOMEM, "host allocation failed");
+    if (options)
+        r->opt = *options;
+    else
+        r->opt.useGraph = 1;
+    if (r->opt.leafSize == 0)
+        r->opt.leafSize = 4;
+    if (r->opt.leafSize > 8)
+        r->opt.leafSize = 8;
+    int rc = OPTPT_OK;
+    cudaError_t e;
+    do {
+        if ((e = cudaStreamCreateWithFlags(&r->ownStream, cudaStreamNonBlocking)) != cudaSuccess) {
+            rc = cudaFail(e, "stream");
+            break;
+        }
+        if ((e = (cudaError_t)uploadSrgbTable()) != cudaSuccess) {
+            rc = cudaFail(e, "sRGB table");
+            break;
+        }
+        const uint32_t nt = s->numTriangles;
+        r->numTris = (int)nt;
+        std::vector<uint32_t> triFlags(nt);
+        for (uint32_t t = 0; t < nt; ++t)
+            triFlags[t] = s->materials[s->matIndices[t]].alphaMode != AM_OPAQUE ? TRI_FLAG_ALPHA : 0u;
+        std::vector<DevMaterial> mats(s->numMaterials);
+        for (uint32_t m = 0; m < s->numMaterials; ++m)
+            mats[m] = toDev(s->materials[m], s->numTextures);
+        std::vector<DevLight> lights(s->numLights);
+        for (uint32_t l = 0; l < s->numLights; ++l)
+            lights[l] = toDev(s->lights[l]);
+        // Emissive triangles, in triangle order (src/gltf_loader.cpp:128-141,
+        // src/renderer.cpp:210-237): emission > 0 or an emissive texture.
+        std::vector<float4> emisV, emisRad;
+        std::vector<float2> emisTc;
+        for (uint32_t t = 0; t < nt; ++t) {
+            const MaterialData &m = s->materials[s->matIndices[t]];
+            if (!(m.emission[0] > 0.0f || m.emission[1] > 0.0f || m.emission[2] > 0.0f || m.hasEmissiveTexture))
+                continue;
+            for (int k = 0; k < 3; ++k) {
+                const int v = s->triIndices[3 * t + k];
+                emisV.push_back(make_float4(s->positions[3 * v], s->positions[3 * v + 1], s->positions[3 * v + 2], 0.0f));
+                emisTc.push_back(s->texCoords ? make_float2(s->texCoords[2 * v], s->texCoords[2 * v + 1])
+                                              : make_float2(0.0f, 0.0f));
+            }
+            int mi = s->matIndices[t];
+            float mf;
+            memcpy(&mf, &mi, 4);
+            emisRad.push_back(make_float4(m.emission[0], m.emission[1], m.emission[2], mf));
+        }
+        r->numEmissive = (int)emisRad.size();
+        r->numLights = (int)s->numLights;
+        std::vector<uint32_t> texels;
+        std::vector<int4> texInfo;
+        for (uint32_t t = 0; t < s->numTextures; ++t) {
+            const optpt_texture &tx = s->textures[t];
+            const int first = (int)texels.size();
+            const size_t cnt = (size_t)tx.width * tx.height;
+            texels.resize(texels.size() + cnt);
+            memcpy(texels.data() + first, tx.rgba, cnt * 4);
+            texInfo.push_back(make_int4(first, (int)tx.width, (int)tx.height,
+                                        (tx.wrapS & 0xF) | ((tx.wrapT & 0xF) << 4) | ((tx.srgb ? 1 : 0) << 8)));
+        }
+        if ((e = upload(r->dPositions, s->positions, (size_t)3 * s->numVertices)) ||
+            (e = upload(r->dNormals, s->normals, s->normals ? (size_t)3 * s->numVertices : 0)) ||
+            (e = upload(r->dTexCoords, s->texCoords, s->texCoords ? (size_t)2 * s->numVertices : 0)) ||
+            (e = upload(r->dTriIndices, s->triIndices, (size_t)3 * nt)) ||
+            (e = upload(r->dMatIndices, s->matIndices, (size_t)nt)) ||
+            (e = upload(r->dTriFlags, triFlags.data(), triFlags.size())) ||
+            (e = upload(r->dMaterials, mats.data(), mats.size())) ||
+            (e = upload(r->dLights, lights.data(), lights.size())) ||
+            (e = upload(r->dLightsPublic, s->lights, (size_t)s->numLights)) ||
+            (e = upload(r->dEmisV, emisV.data(), emisV.size())) ||
+            (e = upload(r->dEmisTc, emisTc.data(), emisTc.size())) ||
+            (e = upload(r->dEmisRad, emisRad.data(), emisRad.size())) ||
+            (e = upload(r->dTexels, texels.data(), texels.size())) ||
+            (e = upload(r->dTexInfo, texInfo.data(), texInfo.size()))) {
+            rc = cudaFail(e, "scene upload");
+            break;
+        }
+        int be = buildBvh(r->dPositions, r->dTriIndices, r->dMatIndices, r->dTriFlags, (int)nt, (int)r->opt.leafSize,
+                          r->bvh, r->ownStream);
+        if (be) {
+            rc = cudaFail((cudaError_t)be, "BVH build");
+            break;
+        }
+        DevScene &ds = r->scene;
+        ds.nodes = r->bvh.nodes;
+        ds.triV = r->bvh.triV;
+        ds.triIndices = r->dTriIndices;
+        ds.normals = r->dNormals;
+        ds.texCoords = r->dTexCoords;
+        ds.materials = r->dMaterials;
+        ds.lights = r->dLights;
+        ds.emisV = r->dEmisV;
+        ds.emisTc = r->dEmisTc;
+        ds.emisRad = r->dEmisRad;
+        ds.texels = r->dTexels;
+        ds.texInfo = r->dTexInfo;
+        ds.numNodes = r->bvh.usedNodes;
+        ds.numTris = (int)nt;
+        ds.numLights = r->numLights;
+        ds.numEmissive = r->numEmissive;
+        if ((e = cudaMalloc((void **)&r->q.counters, sizeof(uint32_t) * CNT_TOTAL)) ||
+            (e = cudaMalloc((void **)&r->q.totals, sizeof(unsigned long long) * 8)) ||
+            (e = cudaMemset(r->q.totals, 0, sizeof(unsigned long long) * 8)) ||
+            (e = cudaMalloc((void **)&r->dState, sizeof(uint32_t) * 4)) ||
+            (e = cudaMalloc((void **)&r->dFrameConst, sizeof(FrameConst)))) {
+            rc = cudaFail(e, "counters");
+            break;
+        }
+        // Frame contract defaults (src/renderer.cpp:24-60, include/renderer.h:137-146).
+        LaunchParams &lp = r->lp;
+        lp.seed = 1;
+        lp.traversable = (uint64_t)(uintptr_t)r->bvh.nodes;
+        lp.lights = r->dLightsPublic;
+        lp.numLights = s->numLights;
+        lp.numEmissiveTriangles = (uint32_t)r->numEmissive;
+        lp.randState = nullptr;
+        lp.vis = 0;
+        lp.toneMapping = 1;
+        lp.toneMappingImpl = 1;
+        lp.gammaCorrection = 1;
+        lp.gammaTerm = 2.2f;
+        lp.maxDepth = s->maxDepth ? s->maxDepth : 8;
+        memcpy(lp.bgColour, s->bgColour, sizeof(lp.bgColour));
+        rc = allocFrame(r, s->resX ? s->resX : 512, s->resY ? s->resY : 512);
+        if (rc)
+            break;
+        const float aspect = (float)r->w / (float)r->h;
+        cameraBasis(s->camEye, s->camTarget, s->camUp, s->camFovYDeg > 0 ? s->camFovYDeg : 40.0f, aspect, lp.U, lp.V,
+                    lp.W);
+        memcpy(lp.eye, s->camEye, sizeof(lp.eye));
+    } while (0);
+    if (rc != OPTPT_OK) {
+        delete r;
+        return rc;
+    }
+    *out = r;
+    return OPTPT_OK;
+}
+
+int optpt_destroy(optpt_renderer *r)
+{
+    if (!r)
+        return OPTPT_OK;
+    cudaDeviceSynchronize();
+    delete r;
+    return OPTPT_OK;
+}
+
+int optpt_setup_output_buffer(optpt_renderer *r, uint32_t width, uint32_t height)
+{
+    if (!r)
+        return fail(OPTPT_ERR_INVALID, "renderer is NULL");
+    if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 27))
+        return fail(OPTPT_ERR_INVALID, "output size out of range");
+    cudaDeviceSynchronize();
+    return allocFrame(r, width, height);
+}
+
+int optpt_setup_camera(optpt_renderer *r, const float eye[3], const float target[3], const float up[3],
+                       float fovYDeg)
+{
+    if (!r || !eye || !target || !up)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if (!(fovYDeg > 0.0f && fovYDeg < 180.0f))
+        return fail(OPTPT_ERR_INVALID, "fovYDeg out of range");
+    const float aspect = r->h ? (float)r->w / (float)r->h : 1.0f;
+    cameraBasis(eye, target, up, fovYDeg, aspect, r->lp.U, r->lp.V, r->lp.W);
+    memcpy(r->lp.eye, eye, sizeof(r->lp.eye));
+    return OPTPT_OK;
+}
+
+int optpt_get_launch_params(const optpt_renderer *r, LaunchParams *out)
+{
+    if (!r || !out)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    *out = r->lp;
+    return OPTPT_OK;
+}
+
+int optpt_set_launch_params(optpt_renderer *r, const LaunchParams *lp)
+{
+    if (!r || !lp)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if (lp->maxDepth < 1 || lp->maxDepth > OPT_MAX_DEPTH)
+        return fail(OPTPT_ERR_INVALID, "maxDepth out of range");
+    if (lp->toneMappingImpl != 0 && lp->toneMappingImpl != 1)
+        return fail(OPTPT_ERR_INVALID, "toneMappingImpl must be 0 or 1");
+    if (lp->sample != r->lp.sample) {
+        uint32_t st[4] = {lp->sample, 0, 0, 0};
+        CUDA_OR_RETURN(cudaDeviceSynchronize(), "set sample");
+        CUDA_OR_RETURN(cudaMemcpy(r->dState, st, sizeof(st), cudaMemcpyHostToDevice), "set sample");
+    }
+    if (lp->maxDepth != r->lp.maxDepth)
+        r->graphDirty = true;
+    LaunchParams &d = r->lp;
+    d.sample = lp->sample;
+    d.seed = lp->seed;
+    memcpy(d.eye, lp->eye, sizeof(d.eye));
+    memcpy(d.U, lp->U, sizeof(d.U));
+    memcpy(d.V, lp->V, sizeof(d.V));
+    memcpy(d.W, lp->W, sizeof(d.W));
+    d.vis = lp->vis;
+    d.toneMapping = lp->toneMapping;
+    d.toneMappingImpl = lp->toneMappingImpl;
+    d.gammaCorrection = lp->gammaCorrection;
+    d.gammaTerm = lp->gammaTerm;
+    d.maxDepth = lp->maxDepth;
+    memcpy(d.bgColour, lp->bgColour, sizeof(d.bgColour));
+    return OPTPT_OK;
+}
+
+int optpt_render(optpt_renderer *r, uint32_t spp, void *stream)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    // The frame constants go up first (from pageable memory, so the host copy
+    // may change as soon as this returns). Whole passes of sppBatch samples
+    // replay the captured graph; a remainder runs as one smaller pass.
+    const FrameConst fc = r->frameConst();
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    const uint32_t passes = spp / r->sppBatch, rem = spp % r->sppBatch;
+    if (r->opt.useGraph && passes) {
+        if ((rc = ensureGraph(r, st ? st : r->ownStream)))
+            return rc;
+        for (uint32_t p = 0; p < passes; ++p)
+            CUDA_OR_RETURN(cudaGraphLaunch(r->graphExec, st), "graph launch");
+    } else {
+        const FrameParams fp = r->frameParams();
+        for (uint32_t p = 0; p < passes; ++p)
+            enqueuePass(r, fp, st, nullptr, nullptr);
+    }
+    if (rem) {
+        FrameParams fp = r->frameParams();
+        fp.sppBatch = rem;
+        fp.numPaths = r->w * r->h * rem;
+        enqueuePass(r, fp, st, nullptr, nullptr);
+    }
+    CUDA_OR_RETURN(cudaGetLastError(), "kernel launch");
+    r->lp.sample += spp;
+    r->hostFbValid = false;
+    return OPTPT_OK;
+}
+
+int optpt_launch(optpt_renderer *r)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if ((rc = optpt_render(r, 1, r->ownStream)))
+        return rc;
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->hostFb.data(), r->acc.frameBuffer, sizeof(float4) * r->w * r->h,
+                                   cudaMemcpyDeviceToHost, r->ownStream),
+                   "frame buffer copy");
+    CUDA_OR_RETURN(cudaStreamSynchronize(r->ownStream), "launch");
+    r->hostFbValid = true;
+    return OPTPT_OK;
+}
+
+const float *optpt_get_frame_buffer(optpt_renderer *r)
+{
+    if (!r || !r->hostFbValid)
+        return nullptr;
+    return r->hostFb.data();
+}
+
+uint32_t optpt_get_sample_count(const optpt_renderer *r) { return r ? r->lp.sample : 0u; }
+
+int optpt_reset_sample_count(optpt_renderer *r)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    cudaDeviceSynchronize();
+    const size_t npix = (size_t)r->w * r->h;
+    CUDA_OR_RETURN(cudaMemset(r->acc.sum, 0, sizeof(Acc4) * npix), "reset");
+    CUDA_OR_RETURN(cudaMemset(r->acc.sumSq, 0, sizeof(Acc4) * npix), "reset");
+    CUDA_OR_RETURN(cudaMemset(r->dState, 0, sizeof(uint32_t) * 4), "reset");
+    r->lp.sample = 0;
+    r->hostFbValid = false;
+    return OPTPT_OK;
+}
+
+int optpt_device_buffers(optpt_renderer *r, float **frameBuffer, float **accumFrameBuffer, double **sum,
+                         double **sumSq)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (frameBuffer)
+        *frameBuffer = (float *)r->acc.frameBuffer;
+    if (accumFrameBuffer)
+        *accumFrameBuffer = (float *)r->acc.accumFrameBuffer;
+    if (sum)
+        *sum = (double *)r->acc.sum;
+    if (sumSq)
+        *sumSq = (double *)r->acc.sumSq;
+    return OPTPT_OK;
+}
+
+int optpt_read_frame_buffer(optpt_renderer *r, float *rgbaHost, void *stream)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (!rgbaHost)
+        return fail(OPTPT_ERR_INVALID, "NULL destination");
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_OR_RETURN(cudaMemcpyAsync(rgbaHost, r->acc.frameBuffer, sizeof(float4) * r->w * r->h,
+                                   cudaMemcpyDeviceToHost, st),
+                   "frame buffer copy");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "frame buffer copy");
+    return OPTPT_OK;
+}
+
+int optpt_read_accum(optpt_renderer *r, double *sumHost, double *sumSqHost, void *stream)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t bytes = sizeof(Acc4) * r->w * r->h;
+    if (sumHost)
+        CUDA_OR_RETURN(cudaMemcpyAsync(sumHost, r->acc.sum, bytes, cudaMemcpyDeviceToHost, st), "accum copy");
+    if (sumSqHost)
+        CUDA_OR_RETURN(cudaMemcpyAsync(sumSqHost, r->acc.sumSq, bytes, cudaMemcpyDeviceToHost, st), "accum copy");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "accum copy");
+    return OPTPT_OK;
+}
+
+int optpt_get_stats(optpt_renderer *r, optpt_stats *out)
+{
+    if (!r || !out)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    unsigned long long t[4] = {0, 0, 0, 0};
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "stats");
+    CUDA_OR_RETURN(cudaMemcpy(t, r->q.totals, sizeof(t), cudaMemcpyDeviceToHost), "stats");
+    out->extensionRays = t[0];
+    out->shadowRays = t[1];
+    out->pathSamples = t[2];
+    out->nanSamples = t[3];
+    out->bvhNodes = (uint32_t)r->bvh.usedNodes;
+    out->bvhLeaves = (uint32_t)r->bvh.numLeaves;
+    out->sppBatch = r->sppBatch;
+    out->blockSize = (uint32_t)r->shape.block;
+    return OPTPT_OK;
+}
+
+int optpt_render_profiled(optpt_renderer *r, uint32_t spp, void *stream, optpt_kernel_times *out)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (!out)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    memset(out, 0, sizeof(*out));
+    cudaStream_t st = (cudaStream_t)stream;
+    const FrameParams fp = r->frameParams();
+    const int maxEv = 3 + 3 * (int)fp.maxDepth;
+    std::vector<cudaEvent_t> ev(maxEv);
+    std::vector<int> kind(maxEv);
+    for (auto &e : ev)
+        CUDA_OR_RETURN(cudaEventCreate(&e), "event");
+    unsigned long long before[2] = {0, 0}, after[2] = {0, 0};
+    const FrameConst fc = r->frameConst();
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "profile");
+    CUDA_OR_RETURN(cudaMemcpy(before, r->q.totals, sizeof(before), cudaMemcpyDeviceToHost), "profile");
+    const uint32_t passes = (spp + r->sppBatch - 1) / r->sppBatch;
+    for (uint32_t p = 0; p < passes; ++p) {
+        FrameParams pf = fp;
+        if (p + 1 == passes && spp % r->sppBatch) {
+            pf.sppBatch = spp % r->sppBatch;
+            pf.numPaths = r->w * r->h * pf.sppBatch;
+        }
+        enqueuePass(r, pf, st, ev.data(), kind.data());
+        CUDA_OR_RETURN(cudaStreamSynchronize(st), "profile pass");
+        for (int k = 0; k + 1 < maxEv; ++k) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            out->ms[kind[k]] += ms;
+            out->launches[kind[k]] += kind[k] == 3 ? 2 : 1;
+        }
+    }
+    r->lp.sample += spp;
+    r->hostFbValid = false;
+    CUDA_OR_RETURN(cudaMemcpy(after, r->q.totals, sizeof(after), cudaMemcpyDeviceToHost), "profile");
+    out->extensionRays = after[0] - before[0];
+    out->shadowRays = after[1] - before[1];
+    for (auto &e : ev)
+        cudaEventDestroy(e);
+    return OPTPT_OK;
+}
+
+int optpt_traversal_counts(optpt_renderer *r, uint32_t spp, void *stream, optpt_traversal_work *out)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (!out)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned long long before[8], after[8];
+    const FrameConst fc = r->frameConst();
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "counts");
+    CUDA_OR_RETURN(cudaMemcpy(before, r->q.totals, sizeof(before), cudaMemcpyDeviceToHost), "counts");
+    const FrameParams fp = r->frameParams();
+    for (uint32_t done = 0; done < spp;) {
+        FrameParams pf = fp;
+        pf.sppBatch = spp - done < r->sppBatch ? spp - done : r->sppBatch;
+        pf.numPaths = r->w * r->h * pf.sppBatch;
+        enqueuePass(r, pf, st, nullptr, nullptr, true);
+        done += pf.sppBatch;
+    }
+    CUDA_OR_RETURN(cudaGetLastError(), "counts launch");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "counts");
+    CUDA_OR_RETURN(cudaMemcpy(after, r->q.totals, sizeof(after), cudaMemcpyDeviceToHost), "counts");
+    r->lp.sample += spp;
+    r->hostFbValid = false;
+    out->extensionRays = after[0] - before[0];
+    out->shadowRays = after[1] - before[1];
+    out->extensionNodes = after[4] - before[4];
+    out->extensionTris = after[5] - before[5];
+    out->shadowNodes = after[6] - before[6];
+    out->shadowTris = after[7] - before[7];
+    return OPTPT_OK;
+}
+
+int optpt_trace(optpt_renderer *r, const float *rays, float *hits, uint32_t n, int anyHit, void *stream)
+{
+    if (!r || (n && (!rays || !hits)))
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if (r->numTris == 0) {
+        std::vector<float4> miss(n, make_float4(INFINITY, 0.0f, 0.0f, 0.0f));
+        for (auto &m : miss) {
+            int neg = -1;
+            memcpy(&m.w, &neg, 4);
+        }
+        CUDA_OR_RETURN(cudaMemcpyAsync(hits, miss.data(), sizeof(float4) * n, cudaMemcpyHostToDevice,
+                                       (cudaStream_t)stream),
+                       "trace");
+        CUDA_OR_RETURN(cudaStreamSynchronize((cudaStream_t)stream), "trace");
+        return OPTPT_OK;
+    }
+    launchTrace(r->scene, (const float4 *)rays, (float4 *)hits, n, anyHit, (cudaStream_t)stream);
+    CUDA_OR_RETURN(cudaGetLastError(), "trace launch");
+    return OPTPT_OK;
+}
+
+int optpt_bvh_leaf_order(optpt_renderer *r, uint32_t *mortonSorted, int32_t *primOrder)
+{
+    if (!r)
+        return fail(OPTPT_ERR_INVALID, "renderer is NULL");
+    if (r->numTris == 0)
+        return OPTPT_OK;
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "leaf order");
+    if (mortonSorted)
+        CUDA_OR_RETURN(cudaMemcpy(mortonSorted, r->bvh.mortonSorted, sizeof(uint32_t) * r->numTris,
+                                  cudaMemcpyDeviceToHost),
+                       "leaf order");
+    if (primOrder)
+        CUDA_OR_RETURN(cudaMemcpy(primOrder, r->bvh.primOrder, sizeof(int32_t) * r->numTris, cudaMemcpyDeviceToHost),
+                       "leaf order");
+    return OPTPT_OK;
+}
+
+int optpt_bvh_nodes(optpt_renderer *r, int32_t *nodes4, uint32_t capacity, uint32_t *numNodes)
+{
+    if (!r || !numNodes)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    *numNodes = (uint32_t)r->bvh.numNodes;
+    if (!nodes4 || r->bvh.numNodes == 0)
+        return OPTPT_OK;
+    if (capacity < (uint32_t)r->bvh.numNodes)
+        return fail(OPTPT_ERR_INVALID, "capacity below the node count");
+    std::vector<BvhNode> nodes(r->bvh.numNodes);
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "nodes");
+    CUDA_OR_RETURN(cudaMemcpy(nodes.data(), r->bvh.nodes, sizeof(BvhNode) * nodes.size(), cudaMemcpyDeviceToHost),
+                   "nodes");
+    for (size_t i = 0; i < nodes.size(); ++i) {
+        nodes4[4 * i] = nodes[i].d.x;
+        nodes4[4 * i + 1] = nodes[i].d.y;
+        nodes4[4 * i + 2] = nodes[i].d.z;
+        nodes4[4 * i + 3] = nodes[i].d.w;
+    }
+    return OPTPT_OK;
+}
+
+int optpt_bsdf_batch(const optpt_bsdf_query *queries, optpt_bsdf_result *results, uint32_t n, void *stream)
+{
+    if (n && (!queries || !results))
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    launchBsdfBatch(queries, results, n, (cudaStream_t)stream);
+    CUDA_OR_RETURN(cudaGetLastError(), "bsdf launch");
+    return OPTPT_OK;
+}
+
+}  // extern "C"

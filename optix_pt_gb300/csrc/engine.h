@@ -1,0 +1,137 @@
+// Internal engine types shared by the build, wavefront and API translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "bvh.cuh"
+
+// Material record used by the shading kernels (derived from MaterialData at
+// upload): 10 x 16 B, read with vector loads.
+struct DevMaterial {
+    float4 baseColour;      // rgb, alpha
+    float4 emissionCutoff;  // emission rgb, alphaCutoff
+    float4 sheen;           // sheenColour rgb, sheenRoughness
+    float4 p0;              // ior, roughness, metallic, specular
+    float4 p1;              // transmissionWeight, subsurfaceWeight, coatWeight, coatRoughness
+    int4 flags;             // category, alphaMode, texture mask bits, 0
+    int4 tex0;              // baseColour, normal, metallicRoughness, emissive texture ids
+    int4 tex1;              // sheenColour, sheenRoughness texture ids, 0, 0
+    float4 tf[6];           // (offset.xy, scale.xy) per texture slot
+};
+enum { TEXBIT_BASE = 1, TEXBIT_NORMAL = 2, TEXBIT_MR = 4, TEXBIT_EMISSIVE = 8, TEXBIT_SHEENC = 16, TEXBIT_SHEENR = 32 };
+
+// Light record used by next-event estimation.
+struct DevLight {
+    float4 p0Type;       // p0.xyz, type (int bits)
+    float4 radianceDist; // radiance.xyz, distance
+    float4 normalCosW;   // normal.xyz, cosWidth
+    float4 cosFalloff;   // cosFalloffStart, 0, 0, 0
+};
+
+struct DevScene {
+    const BvhNode *nodes;
+    const float4 *triV;  // 3 per triangle, leaf order
+    const int *triIndices;  // int3 per primitive (original order)
+    const float *normals;   // float3 per vertex or null
+    const float *texCoords; // float2 per vertex or null
+    const DevMaterial *materials;
+    const DevLight *lights;
+    const float4 *emisV;    // 3 per emissive triangle
+    const float2 *emisTc;   // 3 per emissive triangle
+    const float4 *emisRad;  // radiance.xyz, material index bits
+    const uint32_t *texels; // RGBA8 texels of all textures
+    const int4 *texInfo;    // (first texel, width, height, wrapS | wrapT << 4 | srgb << 8)
+    int numNodes;
+    int numTris;
+    int numLights;
+    int numEmissive;
+};
+
+// Per-frame constants, device resident and uploaded before every render (the
+// reference uploads LaunchParams every frame, src/renderer.cpp:937), so camera
+// or tone-mapping changes need no graph re-capture.
+struct FrameConst {
+    float4 eye;  // xyz; w = seed (uint bits)
+    float4 U;    // xyz; w = vis (int bits)
+    float4 V;    // xyz; w = toneMapping | toneMappingImpl << 1 | gammaCorrection << 2
+    float4 W;    // xyz; w = gammaTerm
+    float4 bg;   // xyz
+};
+
+// Launch-shape parameters baked into a captured pass.
+struct FrameParams {
+    uint32_t w, h, npix, sppBatch, numPaths;
+    uint32_t maxDepth;
+    const uint32_t *state;   // device: [0] = samples accumulated before this pass
+    const FrameConst *fc;    // device
+};
+
+// Device counters: per-depth queue lengths. Depth d uses index d.
+#define CNT_EXT 0
+#define CNT_SHADOW_P 64
+#define CNT_SHADOW_E 128
+#define CNT_TOTAL 192
+#define OPT_MAX_DEPTH 62
+
+// Wavefront buffers (SoA; P = numPaths):
+//   pathT/pathL : float4 per path (throughput + flags, radiance)
+//   rayO/rayD   : two ping-pong ray queues, float4 (origin, path id) and (dir, -)
+//   hit         : float4 (t, u, v, leaf) per queued ray
+//   shO/shD/shC : two shadow queues (point lights, emissive triangles):
+//                 (origin, path id), (dir, tmax), (contribution, blend xi)
+struct WaveBufs {
+    float4 *pathT, *pathL;
+    float4 *rayO[2], *rayD[2];
+    float4 *hit;
+    float4 *shO[2], *shD[2], *shC[2];
+    uint32_t *counters;              // CNT_TOTAL entries
+    unsigned long long *totals;      // 0 ext rays, 1 shadow rays, 2 samples, 3 NaN samples,
+                                     // 4-5 ext nodes/tris, 6-7 shadow nodes/tris (counting mode)
+};
+
+// FP64 per-pixel accumulator (xyz used), 32-byte aligned for vector access.
+struct alignas(32) Acc4 {
+    double x, y, z, w;
+};
+
+struct AccumBufs {
+    Acc4 *sum, *sumSq;
+    float4 *frameBuffer, *accumFrameBuffer;
+};
+
+struct LaunchShape {
+    int gridGenerate, gridExtend, gridShade, gridShadow, gridAccum;
+    int block;
+};
+
+// wavefront.cu
+void launchGenerate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs &q, cudaStream_t st);
+// count = true runs the counting variant (BVH nodes and triangles visited
+// added to totals[4..5] for extension rays, totals[6..7] for shadow rays).
+void launchExtend(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
+                  cudaStream_t st, bool count = false);
+void launchShade(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
+                 cudaStream_t st);
+void launchShadow(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
+                  int which, cudaStream_t st, bool count = false);
+void launchAccumulate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs &q, const AccumBufs &a,
+                      cudaStream_t st);
+void launchAdvance(const FrameParams &fp, uint32_t *state, cudaStream_t st);
+void launchTrace(const DevScene &s, const float4 *rays, float4 *hits, uint32_t n, int anyHit, cudaStream_t st);
+void launchBsdfBatch(const void *queries, void *results, uint32_t n, cudaStream_t st);
+int occupancyGrid(int kernelId, int block);  // persistent grid for a kernel class
+
+// bvh_build.cu
+struct BvhBuild {
+    BvhNode *nodes;        // n - 1 slots (holes where subtrees collapsed to leaves)
+    float4 *triV;          // 3 * n
+    uint32_t *mortonSorted;
+    int *primOrder;
+    int numNodes;          // slots allocated
+    int usedNodes;         // internal nodes emitted
+    int numLeaves;
+};
+// Builds the LBVH on `st`. positions/triIndices/matIndices are device arrays;
+// triFlags (device, per primitive) go to triV[3i+2].w. Returns 0 or a CUDA error.
+int buildBvh(const float *positions, const int *triIndices, const int *matIndices, const uint32_t *triFlags,
+             int numTris, int leafSize, BvhBuild &out, cudaStream_t st);
+void freeBvh(BvhBuild &b);

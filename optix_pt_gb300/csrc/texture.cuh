@@ -1,0 +1,72 @@
+// Software texture sampling of RGBA8 images stored as packed texels in HBM.
+// Stands in for the reference's hardware texture objects (src/renderer.cpp:
+// 1439-1757: normalized coordinates, linear or point filter, wrap/clamp/mirror
+// per axis, sRGB decode for colour textures). Filter weights are FP32 rather
+// than the texture unit's 8-bit fixed point, so the host oracle reproduces the
+// result exactly.
+#pragma once
+#include "common.cuh"
+
+#define TEX_WRAP_REPEAT 0
+#define TEX_WRAP_CLAMP 1
+#define TEX_WRAP_MIRROR 2
+
+// sRGB -> linear for the 256 byte values (IEC 61966-2-1), filled by the host.
+__constant__ float c_srgbToLinear[256];
+
+OPT_D int wrapTexel(int i, int n, int mode)
+{
+    if (mode == TEX_WRAP_CLAMP)
+        return min(max(i, 0), n - 1);
+    if (mode == TEX_WRAP_MIRROR) {
+        int p = 2 * n;
+        int m = ((i % p) + p) % p;
+        return m < n ? m : p - 1 - m;
+    }
+    return ((i % n) + n) % n;
+}
+
+OPT_D float4 texelToFloat(uint32_t t, bool srgb)
+{
+    float4 c;
+    if (srgb) {
+        c.x = c_srgbToLinear[t & 0xFFu];
+        c.y = c_srgbToLinear[(t >> 8) & 0xFFu];
+        c.z = c_srgbToLinear[(t >> 16) & 0xFFu];
+    } else {
+        c.x = (float)(t & 0xFFu) * (1.0f / 255.0f);
+        c.y = (float)((t >> 8) & 0xFFu) * (1.0f / 255.0f);
+        c.z = (float)((t >> 16) & 0xFFu) * (1.0f / 255.0f);
+    }
+    c.w = (float)(t >> 24) * (1.0f / 255.0f);
+    return c;
+}
+
+// info = (first texel, width, height, wrapS | wrapT << 4 | srgb << 8 | point << 9)
+OPT_D float4 sampleTexture(const uint32_t *__restrict__ texels, int4 info, float u, float v)
+{
+    const int W = info.y, H = info.z;
+    const int ws = info.w & 0xF, wt = (info.w >> 4) & 0xF;
+    const bool srgb = (info.w >> 8) & 1, point = (info.w >> 9) & 1;
+    const uint32_t *img = texels + info.x;
+    float x = u * (float)W, y = v * (float)H;
+    if (point) {
+        int ix = wrapTexel((int)floorf(x), W, ws), iy = wrapTexel((int)floorf(y), H, wt);
+        return texelToFloat(__ldg(img + iy * W + ix), srgb);
+    }
+    x -= 0.5f;
+    y -= 0.5f;
+    float fx0 = floorf(x), fy0 = floorf(y);
+    float ax = x - fx0, ay = y - fy0;
+    int x0 = (int)fx0, y0 = (int)fy0;
+    int xa = wrapTexel(x0, W, ws), xb = wrapTexel(x0 + 1, W, ws);
+    int ya = wrapTexel(y0, H, wt), yb = wrapTexel(y0 + 1, H, wt);
+    float4 c00 = texelToFloat(__ldg(img + ya * W + xa), srgb), c10 = texelToFloat(__ldg(img + ya * W + xb), srgb);
+    float4 c01 = texelToFloat(__ldg(img + yb * W + xa), srgb), c11 = texelToFloat(__ldg(img + yb * W + xb), srgb);
+    float4 r;
+    r.x = (c00.x + (c10.x - c00.x) * ax) + ((c01.x + (c11.x - c01.x) * ax) - (c00.x + (c10.x - c00.x) * ax)) * ay;
+    r.y = (c00.y + (c10.y - c00.y) * ax) + ((c01.y + (c11.y - c01.y) * ax) - (c00.y + (c10.y - c00.y) * ax)) * ay;
+    r.z = (c00.z + (c10.z - c00.z) * ax) + ((c01.z + (c11.z - c01.z) * ax) - (c00.z + (c10.z - c00.z) * ax)) * ay;
+    r.w = (c00.w + (c10.w - c00.w) * ax) + ((c01.w + (c11.w - c01.w) * ax) - (c00.w + (c10.w - c00.w) * ax)) * ay;
+    return r;
+}

@@ -1,0 +1,128 @@
+// BVH2 traversal kernels' device routines: closest hit (the radiance ray of
+// cu/device_programs.cu:63 with __anyhit__radiance's alpha test, :108-166)
+// and occlusion (the shadow ray of cu/path_tracer.cu:396,485 with
+// __anyhit__shadow, cu/device_programs.cu:180-219).
+#pragma once
+#include <climits>
+#include "bvh.cuh"
+
+#define BVH_STACK 64  // >= LBVH depth: 30 Morton bits + log2(duplicate run)
+
+struct HitRec {
+    float t, u, v;
+    int leaf;  // leaf-order triangle index, -1 = miss
+};
+
+OPT_D float safeInv(float d) { return 1.0f / (fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d)); }
+
+// Slab test of one child box; returns the entry distance or +inf on a miss.
+// The exit distance is widened by 4e-7 relative (Ize, "Robust BVH Ray
+// Traversal", JCGT 2(2), 2013) so rounding never culls a box whose triangle
+// the watertight test would hit.
+OPT_D float boxEntry(float lox, float hix, float loy, float hiy, float loz, float hiz, float3 o, float3 inv,
+                     float tmin, float tmax)
+{
+    float x0 = (lox - o.x) * inv.x, x1 = (hix - o.x) * inv.x;
+    float y0 = (loy - o.y) * inv.y, y1 = (hiy - o.y) * inv.y;
+    float z0 = (loz - o.z) * inv.z, z1 = (hiz - o.z) * inv.z;
+    float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
+    float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1)) * 1.0000004f;
+    return tn <= fminf(tf, tmax) ? tn : __int_as_float(0x7f800000);
+}
+
+// Walks the BVH. ANY = true stops at the first accepted hit (occlusion).
+// `alpha(leaf, prim, u, v)` decides whether a candidate on a triangle with
+// TRI_FLAG_ALPHA is kept (the any-hit programs' optixIgnoreIntersection).
+struct NoCount {
+    OPT_D void node() {}
+    OPT_D void tri() {}
+};
+struct Count {
+    uint32_t nodes = 0, tris = 0;
+    OPT_D void node() { ++nodes; }
+    OPT_D void tri() { ++tris; }
+};
+
+template <bool ANY, class AlphaFn, class Counter = NoCount>
+OPT_D bool traverse(const BvhNode *__restrict__ nodes, const float4 *__restrict__ triV, float3 o, float3 d,
+                    float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &&ctr = Counter())
+{
+    hit.leaf = -1;
+    if (nodes == nullptr)  // empty scene
+        return false;
+    const RayPre pre = rayPrepare(o, d);
+    const float3 inv = mk3(safeInv(d.x), safeInv(d.y), safeInv(d.z));
+    int stack[BVH_STACK];
+    int sp = 0;
+    int node = 0;
+    float tcur = tmax;
+    int bestPrim = INT_MAX;
+    // The node budget bounds the walk even on a corrupted tree (a valid BVH of
+    // n triangles visits at most 2n nodes).
+    for (int budget = 1 << 26; budget > 0; --budget) {
+        ctr.node();
+        const BvhNode *N = nodes + node;
+        const float4 a = __ldg(&N->a), b = __ldg(&N->b), c = __ldg(&N->c);
+        const int4 r = __ldg(&N->d);
+        float tl = r.x >= 0 ? boxEntry(a.x, a.y, a.z, a.w, c.x, c.y, o, inv, tmin, tcur) : __int_as_float(0x7f800000);
+        float tr = r.y >= 0 ? boxEntry(b.x, b.y, b.z, b.w, c.z, c.w, o, inv, tmin, tcur) : __int_as_float(0x7f800000);
+        bool hl = tl != __int_as_float(0x7f800000), hr = tr != __int_as_float(0x7f800000);
+        // Leaf children are intersected on the spot.
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const bool h = side == 0 ? hl : hr;
+            const int cnt = side == 0 ? r.z : r.w;
+            if (!h || cnt == 0)
+                continue;
+            const int first = side == 0 ? r.x : r.y;
+            for (int k = first; k < first + cnt; ++k) {
+                ctr.tri();
+                const float4 t0 = __ldg(triV + 3 * k), t1 = __ldg(triV + 3 * k + 1), t2 = __ldg(triV + 3 * k + 2);
+                float t, u, v;
+                if (!intersectTri(pre, f3of4(t0), f3of4(t1), f3of4(t2), tmin, tcur, t, u, v))
+                    continue;
+                const int prim = __float_as_int(t0.w);
+                if ((__float_as_uint(t2.w) & TRI_FLAG_ALPHA) && !alpha(k, prim, u, v))
+                    continue;
+                if (ANY) {
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    hit.leaf = k;
+                    return true;
+                }
+                if (t < tcur || prim < bestPrim) {
+                    tcur = t;
+                    bestPrim = prim;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    hit.leaf = k;
+                }
+            }
+            if (side == 0)
+                hl = false;
+            else
+                hr = false;
+        }
+        if (hl && hr) {
+            const bool leftFirst = tl <= tr;
+            if (sp < BVH_STACK)
+                stack[sp++] = leftFirst ? r.y : r.x;
+            node = leftFirst ? r.x : r.y;
+        } else if (hl) {
+            node = r.x;
+        } else if (hr) {
+            node = r.y;
+        } else {
+            if (sp == 0)
+                break;
+            node = stack[--sp];
+        }
+    }
+    return hit.leaf >= 0;
+}
+
+struct NoAlpha {
+    OPT_D bool operator()(int, int, float, float) const { return true; }
+};

@@ -1,0 +1,786 @@
+// Wavefront path-tracing kernels: generate -> (extend -> shade -> shadow) x depth
+// -> accumulate. Together they replace the reference's OptiX megakernel
+// (cu/device_programs.cu:15-106 raygen loop, cu/path_tracer.cu:17-582
+// closest-hit shading with next-event estimation, the any-hit/miss programs
+// of cu/device_programs.cu:108-223, and cu/light_sampling.cu:6-81).
+//
+// Paths live in SoA buffers indexed by path id (= sample-in-batch * npix +
+// pixel). Each bounce's rays are a compacted queue: shade appends survivors
+// with one atomic per warp (ballot + popc prefix). Kernels are persistent:
+// grids of a few blocks per SM loop over the queue length, which they read
+// from device memory, so the whole bounce loop can be captured in one graph.
+#include <cfloat>
+#include "bsdf.cuh"
+#include "engine.h"
+#include "texture.cuh"
+#include "trace.cuh"
+
+
+
+namespace {
+
+struct PcgSource {
+    Pcg32 *r;
+    OPT_D float next() { return r->uniform(); }
+};
+
+OPT_D float4 mk4(float3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// Appends `want` lanes' records to a queue: one atomicAdd per warp, slots
+// ordered by lane. Must be reached by all 32 lanes.
+template <int N> OPT_D void warpPush(bool want, uint32_t *counter, float4 *const (&dst)[N], const float4 (&val)[N])
+{
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (m == 0u)
+        return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader)
+        base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (want) {
+        const uint32_t slot = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+            dst[k][slot] = val[k];
+    }
+}
+
+// Alpha test of a candidate (cu/device_programs.cu:108-166 radiance,
+// :180-219 shadow). The any-hit programs interpolate the texture coordinate
+// without the texture transform (:126-130).
+struct AlphaTest {
+    const float4 *triV;
+    const DevMaterial *materials;
+    const int *triIndices;
+    const float *texCoords;
+    const uint32_t *texels;
+    const int4 *texInfo;
+    uint32_t seed, pixel, sample, depth;
+    float shadowXi;  // < 0: radiance ray (blend uniform hashed per candidate)
+    OPT_D bool operator()(int leaf, int prim, float u, float v) const
+    {
+        const int matIdx = __float_as_int(__ldg(&triV[3 * leaf + 1]).w);
+        const DevMaterial &M = materials[matIdx];
+        const int4 fl = __ldg(&M.flags);
+        const float4 bc = __ldg(&M.baseColour);
+        float alpha = bc.w;
+        if ((fl.z & TEXBIT_BASE) && texCoords) {
+            const int i0 = __ldg(triIndices + 3 * prim), i1 = __ldg(triIndices + 3 * prim + 1),
+                      i2 = __ldg(triIndices + 3 * prim + 2);
+            const float w = 1.0f - u - v;
+            const float tu = w * __ldg(texCoords + 2 * i0) + u * __ldg(texCoords + 2 * i1) +
+                             v * __ldg(texCoords + 2 * i2);
+            const float tv = w * __ldg(texCoords + 2 * i0 + 1) + u * __ldg(texCoords + 2 * i1 + 1) +
+                             v * __ldg(texCoords + 2 * i2 + 1);
+            alpha *= sampleTexture(texels, __ldg(texInfo + __ldg(&M.tex0).x), tu, tv).w;
+        }
+        if (fl.y == AM_MASK)
+            return !(alpha < __ldg(&M.emissionCutoff).w);
+        if (fl.y == AM_BLEND) {
+            const float xi = shadowXi >= 0.0f ? shadowXi : blendUniform(seed, pixel, sample, depth, (uint32_t)prim);
+            return !(xi > alpha);
+        }
+        return true;
+    }
+};
+
+OPT_D AlphaTest makeAlpha(const DevScene &s, uint32_t seed, uint32_t pixel, uint32_t sample, uint32_t depth,
+                          float shadowXi)
+{
+    return AlphaTest{s.triV, s.materials, s.triIndices, s.texCoords, s.texels, s.texInfo,
+                     seed, pixel, sample, depth, shadowXi};
+}
+
+// ------------------------------------------------------------------ generate
+// Camera ray with pixel jitter (cu/device_programs.cu:40-53).
+__global__ void __launch_bounds__(256) kGenerate(FrameParams fp, WaveBufs q)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t sampleBase = __ldg(fp.state);
+    const float4 e4 = __ldg(&fp.fc->eye), u4 = __ldg(&fp.fc->U), v4 = __ldg(&fp.fc->V), w4 = __ldg(&fp.fc->W);
+    const uint32_t seed = __float_as_uint(e4.w);
+    const float3 eye = f3of4(e4), camU = f3of4(u4), camV = f3of4(v4), camW = f3of4(w4);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < fp.numPaths; p += stride) {
+        const uint32_t pixel = p % fp.npix, b = p / fp.npix;
+        const uint32_t x = pixel % fp.w, y = pixel / fp.w;
+        Pcg32 rng = pathRng(seed, pixel, sampleBase + b, 0u);
+        const float jx = rng.uniform(), jy = rng.uniform();
+        const float fx = (float)x + jx, fy = (float)y + jy;
+        const float ndcx = (fx / (float)fp.w) * 2.0f + -1.0f;
+        const float ndcy = (fy / (float)fp.h) * -2.0f + 1.0f;
+        const float3 dir = normalize3(ndcx * camU + ndcy * camV + camW);
+        q.rayO[1][p] = mk4(eye, __int_as_float((int)p));
+        q.rayD[1][p] = mk4(dir, 0.0f);
+        q.pathT[p] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+        q.pathL[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        q.counters[CNT_EXT + 1] = fp.numPaths;
+}
+
+// ------------------------------------------------------------------ extend
+// Closest hit of each queued ray: tmin 0, tmax 1e16 (cu/device_programs.cu:63).
+// Adds per-thread traversal counts to totals[slot], [slot + 1] (counting mode).
+OPT_D void flushCounts(const Count &c, unsigned long long *totals, int slot)
+{
+    unsigned long long n = c.nodes, t = c.tris;
+    for (int off = 16; off > 0; off >>= 1) {
+        n += __shfl_down_sync(0xffffffffu, n, off);
+        t += __shfl_down_sync(0xffffffffu, t, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(totals + slot, n);
+        atomicAdd(totals + slot + 1, t);
+    }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(256) kExtend(DevScene s, FrameParams fp, WaveBufs q, int depth)
+{
+    const uint32_t count = q.counters[CNT_EXT + depth];
+    const int cur = depth & 1;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t sampleBase = __ldg(fp.state);
+    const uint32_t seed = __float_as_uint(__ldg(&fp.fc->eye).w);
+    typename std::conditional<COUNT, Count, NoCount>::type ctr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const float4 ro = q.rayO[cur][i], rd = q.rayD[cur][i];
+        const uint32_t path = (uint32_t)__float_as_int(ro.w);
+        const AlphaTest at = makeAlpha(s, seed, path % fp.npix, sampleBase + path / fp.npix, (uint32_t)depth, -1.0f);
+        HitRec h;
+        const bool hit = traverse<false>(s.nodes, s.triV, f3of4(ro), f3of4(rd), 0.0f, 1e16f, h, at, ctr);
+        q.hit[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.leaf))
+                       : make_float4(__int_as_float(0x7f800000), 0.0f, 0.0f, __int_as_float(-1));
+    }
+    if constexpr (COUNT)
+        flushCounts(ctr, q.totals, 4);
+}
+
+// ------------------------------------------------------------------ shade
+struct LightSampleD {
+    float3 dir, Li;
+    float pdf, dist;
+};
+
+// point_sample / directional_sample / spot_sample (cu/light_sampling.cu:6-59)
+OPT_D LightSampleD sampleLight(const DevLight &L, float3 p)
+{
+    LightSampleD r;
+    const float4 a = __ldg(&L.p0Type), b = __ldg(&L.radianceDist), c = __ldg(&L.normalCosW);
+    const int type = __float_as_int(a.w);
+    const float3 rad = f3of4(b);
+    r.pdf = 1.0f;
+    if (type == 1) {
+        const float3 n = f3of4(c);
+        const float3 pos = p + (-n * b.w);
+        r.dir = -n;
+        r.Li = rad;
+        r.dist = length3(pos - p);
+    } else {
+        float3 dir = f3of4(a) - p;
+        const float dist = length3(dir);
+        dir = dir / dist;
+        r.dir = dir;
+        r.dist = dist;
+        if (type == 2) {  // falloff (include/sampling.h:64-77)
+            const float cw = c.w, cfs = __ldg(&L.cosFalloff).x;
+            const float ct = dot3(f3of4(c), -dir);
+            float fo;
+            if (ct < cw)
+                fo = 0.0f;
+            else if (ct > cfs)
+                fo = 1.0f;
+            else {
+                const float dl = (ct - cw) / (cfs - cw);
+                fo = (dl * dl) * (dl * dl);
+            }
+            r.Li = rad * fo / (dist * dist);
+        } else {
+            r.Li = rad / (dist * dist);
+        }
+    }
+    return r;
+}
+
+OPT_D bool nonzeroOrNonfinite(float3 c)
+{
+    return c.x != 0.0f || c.y != 0.0f || c.z != 0.0f || !isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z);
+}
+
+OPT_D float2 interpTc(const DevScene &s, int prim, float u, float v)
+{
+    const int i0 = __ldg(s.triIndices + 3 * prim), i1 = __ldg(s.triIndices + 3 * prim + 1),
+              i2 = __ldg(s.triIndices + 3 * prim + 2);
+    const float2 t0 = __ldg(reinterpret_cast<const float2 *>(s.texCoords) + i0);
+    const float2 t1 = __ldg(reinterpret_cast<const float2 *>(s.texCoords) + i1);
+    const float2 t2 = __ldg(reinterpret_cast<const float2 *>(s.texCoords) + i2);
+    const float w = 1.0f - u - v;
+    return make_float2(w * t0.x + u * t1.x + v * t2.x, w * t0.y + u * t1.y + v * t2.y);
+}
+
+OPT_D float4 texAt(const DevScene &s, int tex, float4 tf, float2 tc)
+{
+    const float x = tc.x * tf.z + tf.x, y = tc.y * tf.w + tf.y;  // uv * scale + offset
+    return sampleTexture(s.texels, __ldg(s.texInfo + tex), x, y);
+}
+
+// Closest-hit shading, next-event estimation and continuation
+// (cu/path_tracer.cu:17-582), miss (cu/device_programs.cu:168-174).
+__global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBufs q, int depth)
+{
+    const uint32_t count = q.counters[CNT_EXT + depth];
+    const int lane = threadIdx.x & 31;
+    const uint32_t warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nWarps = (gridDim.x * blockDim.x) >> 5;
+    const int cur = depth & 1, nxt = cur ^ 1;
+    const uint32_t sampleBase = __ldg(fp.state);
+    const uint32_t seed = __float_as_uint(__ldg(&fp.fc->eye).w);
+    const int vis = __float_as_int(__ldg(&fp.fc->U).w);
+    const float3 bg = f3of4(__ldg(&fp.fc->bg));
+    float4 *const nextQ[2] = {q.rayO[nxt], q.rayD[nxt]};
+    float4 *const shPQ[3] = {q.shO[0], q.shD[0], q.shC[0]};
+    float4 *const shEQ[3] = {q.shO[1], q.shD[1], q.shC[1]};
+
+    for (uint32_t base = warpId * 32u; base < count; base += nWarps * 32u) {
+        const uint32_t i = base + (uint32_t)lane;
+        bool cont = false, wantP = false, wantE = false;
+        float4 nxtRay[2], shP[3], shE[3];
+        if (i < count) {
+            const float4 ro = q.rayO[cur][i], rd = q.rayD[cur][i];
+            const uint32_t path = (uint32_t)__float_as_int(ro.w);
+            const float4 hrec = q.hit[i];
+            float4 T4 = q.pathT[path];
+            float3 T = f3of4(T4);
+            float3 L = f3of4(q.pathL[path]);
+            uint32_t flags = __float_as_uint(T4.w);
+            const float3 rayDir = f3of4(rd), rayOrig = f3of4(ro);
+            const int leaf = __float_as_int(hrec.w);
+            if (leaf < 0) {
+                L = L + bg * T;
+            } else {
+                const uint32_t pixel = path % fp.npix, sample = sampleBase + path / fp.npix;
+                Pcg32 rng = pathRng(seed, pixel, sample, (uint32_t)depth);
+                PcgSource U{&rng};
+                const float4 t0 = __ldg(&s.triV[3 * leaf]), t1 = __ldg(&s.triV[3 * leaf + 1]),
+                             t2 = __ldg(&s.triV[3 * leaf + 2]);
+                const int prim = __float_as_int(t0.w), matIdx = __float_as_int(t1.w);
+                const DevMaterial &M = s.materials[matIdx];
+                const float4 mbc = __ldg(&M.baseColour), mem = __ldg(&M.emissionCutoff), msh = __ldg(&M.sheen);
+                const float4 mp0 = __ldg(&M.p0), mp1 = __ldg(&M.p1);
+                const int4 mfl = __ldg(&M.flags);
+                const float u = hrec.y, v = hrec.z;
+
+                float2 tc = make_float2(0.0f, 0.0f);
+                if (mfl.z != 0 && s.texCoords)
+                    tc = interpTc(s, prim, u, v);
+
+                float3 hitPoint = rayOrig + hrec.x * rayDir;
+                const float3 v0 = f3of4(t0), v1 = f3of4(t1), v2 = f3of4(t2);
+                const float3 Ng = normalize3(cross3(v1 - v0, v2 - v0));
+                float3 interpN = Ng;
+                bool hasN = false;
+                if (s.normals) {
+                    const int i0 = __ldg(s.triIndices + 3 * prim), i1 = __ldg(s.triIndices + 3 * prim + 1),
+                              i2 = __ldg(s.triIndices + 3 * prim + 2);
+                    const float3 n0 = mk3(__ldg(s.normals + 3 * i0), __ldg(s.normals + 3 * i0 + 1),
+                                          __ldg(s.normals + 3 * i0 + 2));
+                    const float3 n1 = mk3(__ldg(s.normals + 3 * i1), __ldg(s.normals + 3 * i1 + 1),
+                                          __ldg(s.normals + 3 * i1 + 2));
+                    const float3 n2 = mk3(__ldg(s.normals + 3 * i2), __ldg(s.normals + 3 * i2 + 1),
+                                          __ldg(s.normals + 3 * i2 + 2));
+                    interpN = normalize3((1.0f - u - v) * n0 + u * n1 + v * n2);
+                    hasN = true;
+                }
+                float3 normal = interpN;
+                if ((mfl.z & TEXBIT_NORMAL) && s.texCoords) {
+                    // Tangent-space normal map (cu/path_tracer.cu:64-144).
+                    float3 sn = f3of4(texAt(s, __ldg(&M.tex0).y, __ldg(&M.tf[1]), tc));
+                    sn = normalize3(sn * 2.0f - mk3s(1.0f));
+                    const int i0 = __ldg(s.triIndices + 3 * prim), i1 = __ldg(s.triIndices + 3 * prim + 1),
+                              i2 = __ldg(s.triIndices + 3 * prim + 2);
+                    const float2 w0 = __ldg(reinterpret_cast<const float2 *>(s.texCoords) + i0);
+                    const float2 w1 = __ldg(reinterpret_cast<const float2 *>(s.texCoords) + i1);
+                    const float2 w2 = __ldg(reinterpret_cast<const float2 *>(s.texCoords) + i2);
+                    const float3 e1 = v1 - v0, e2 = v2 - v0;
+                    const float2 d1 = make_float2(w1.x - w0.x, w1.y - w0.y), d2 = make_float2(w2.x - w0.x, w2.y - w0.y);
+                    const float f = 1.0f / (d1.x * d2.y - d2.x * d1.y);
+                    float3 tl = mk3(f * (d2.y * e1.x - d1.y * e2.x), f * (d2.y * e1.y - d1.y * e2.y),
+                                    f * (d2.y * e1.z - d1.y * e2.z));
+                    tl = normalize3(tl);
+                    const float3 N = hasN ? interpN : Ng;
+                    const float3 Tg = normalize3(tl - dot3(tl, N) * N);
+                    const float3 B = cross3(N, Tg);
+                    normal = normalize3(mk3(Tg.x * sn.x + B.x * sn.y + N.x * sn.z, Tg.y * sn.x + B.y * sn.y + N.y * sn.z,
+                                            Tg.z * sn.x + B.z * sn.y + N.z * sn.z));
+                }
+
+                // Material inputs after textures (cu/path_tracer.cu:165-229).
+                float3 albedo = f3of4(mbc);
+                float alpha = mbc.w;
+                if (mfl.z & TEXBIT_BASE) {
+                    const float4 bt = texAt(s, __ldg(&M.tex0).x, __ldg(&M.tf[0]), tc);
+                    albedo = albedo * f3of4(bt);
+                    alpha *= bt.w;
+                }
+                float occlusion = 1.0f, roughness = mp0.y, metallic = mp0.z;
+                if (mfl.z & TEXBIT_MR) {
+                    const float4 mr = texAt(s, __ldg(&M.tex0).z, __ldg(&M.tf[2]), tc);
+                    occlusion *= mr.x;
+                    roughness *= mr.y;
+                    metallic = mr.z < 0.04f ? 0.0f : metallic * mr.z;
+                }
+                float3 emission = f3of4(mem);
+                if (mfl.z & TEXBIT_EMISSIVE)
+                    emission = emission * f3of4(texAt(s, __ldg(&M.tex0).w, __ldg(&M.tf[3]), tc));
+                float3 sheenColour = f3of4(msh);
+                if (mfl.z & TEXBIT_SHEENC)
+                    sheenColour = sheenColour * f3of4(texAt(s, __ldg(&M.tex1).x, __ldg(&M.tf[4]), tc));
+                float sheenRoughness = msh.w;
+                if (mfl.z & TEXBIT_SHEENR)
+                    sheenRoughness *= texAt(s, __ldg(&M.tex1).y, __ldg(&M.tf[5]), tc).w;
+
+                const bsdf::CatIn ci{(uint32_t)mfl.x, mp1.z, mp1.w, mp1.x, mp0.w, mp1.y};
+                float cw;
+                const uint32_t cat = bsdf::categorise(ci, -rayDir, normal, roughness, metallic, emission, sheenColour,
+                                                      sheenRoughness, U, cw);
+                const bool spec = (cat & MF_SPECULAR) != 0;
+
+                if (vis != 0) {
+                    // Material visualisation AOVs (cu/path_tracer.cu:252-315).
+                    switch (vis) {
+                    case 1: L = mk3s(metallic); break;
+                    case 2: L = mk3s(roughness); break;
+                    case 3: L = mk3s(occlusion); break;
+                    case 4: L = emission; break;
+                    case 5: L = normal * 0.5f + mk3s(0.5f); break;
+                    case 6: L = Ng * 0.5f + mk3s(0.5f); break;
+                    case 7: L = albedo; break;
+                    case 8: L = metallic * albedo * mk3s(mp0.w); break;
+                    case 10: L = sheenColour; break;
+                    case 11: L = mk3s(sheenRoughness); break;
+                    case 12: L = mk3s(alpha); break;
+                    default: break;
+                    }
+                } else {
+                    if (!spec)
+                        hitPoint = hitPoint - rayDir * OPT_SHADOW_BIAS;
+                    if (cat & MF_EMISSION) {
+                        if (dot3(rayDir, normal) < 0.0f && (depth == 1 || (flags & 1u)))
+                            L = L + (emission + albedo * T);
+                    } else {
+                        flags = spec ? 1u : 0u;
+                        const bsdf::MatMR m = bsdf::makeMatMR(albedo, mp0.x, metallic, sheenColour, cat, normal,
+                                                              roughness, mp1.w, msh.w);
+                        const float3 wo = -rayDir;
+                        if (!spec && s.numLights != 0) {
+                            // Point / directional / spot NEE (cu/path_tracer.cu:375-412).
+                            const float lu = U.next();
+                            const int li = min((int)(lu * (float)s.numLights), s.numLights - 1);
+                            const float selPdf = 1.0f / (float)s.numLights;
+                            const LightSampleD ls = sampleLight(s.lights[li], hitPoint);
+                            const float cosX = fmaxf(dot3(normal, ls.dir), 0.0f);
+                            const float sxi = U.next();
+                            const float3 brdf = bsdf::evalBrdf(m, ls.dir, wo, U);
+                            const float3 colour = brdf * ls.Li * cosX / ls.pdf / selPdf;
+                            const float3 c = colour * T;
+                            if (nonzeroOrNonfinite(c)) {
+                                wantP = true;
+                                shP[0] = mk4(hitPoint, __int_as_float((int)path));
+                                shP[1] = mk4(ls.dir, ls.dist - OPT_SCENE_EPSILON);
+                                shP[2] = mk4(c, sxi);
+                            }
+                        }
+                        if (!spec && s.numEmissive != 0) {
+                            // Emissive-triangle NEE (cu/path_tracer.cu:415-515).
+                            const int ei = min((int)(U.next() * (float)s.numEmissive), s.numEmissive - 1);
+                            const float selPdf = 1.0f / (float)s.numEmissive;
+                            float xa = U.next(), xb = U.next();
+                            if (xa + xb > 1.0f) {
+                                xa = 1.0f - xa;
+                                xb = 1.0f - xb;
+                            }
+                            const float3 p0 = f3of4(__ldg(&s.emisV[3 * ei])), p1 = f3of4(__ldg(&s.emisV[3 * ei + 1])),
+                                         p2 = f3of4(__ldg(&s.emisV[3 * ei + 2]));
+                            const float3 e1 = p1 - p0, e2 = p2 - p0;
+                            const float3 lightPos = p0 + e1 * xa + e2 * xb;
+                            const float3 lnv = cross3(e1, e2);
+                            const float3 ln = normalize3(lnv);
+                            const float pdfA = 1.0f / (length3(lnv) * 0.5f);
+                            const float3 lvec = lightPos - hitPoint;
+                            const float dist = length3(lvec);
+                            const float3 ldir = lvec / dist;
+                            const float cosY = fmaxf(0.0f, dot3(ln, -ldir));
+                            const float4 er = __ldg(&s.emisRad[ei]);
+                            float3 Le = f3of4(er);
+                            const DevMaterial &EM = s.materials[__float_as_int(er.w)];
+                            if ((__ldg(&EM.flags).z & TEXBIT_EMISSIVE) && s.texCoords) {
+                                // Barycentrics of the light point (include/barycentrics.h:17-44); the
+                                // hit material's transform is applied, as in the reference (:466-468).
+                                const float3 mm = cross3(p1 - p0, p2 - p0);
+                                const float ax = fabsf(mm.x), ay = fabsf(mm.y), az = fabsf(mm.z);
+                                float nu, nv, ood;
+                                auto area2 = [](float x1, float y1, float x2, float y2, float x3, float y3) {
+                                    return (x1 - x2) * (y2 - y3) - (x2 - x3) * (y1 - y2);
+                                };
+                                if (ax >= ay && ax >= az) {
+                                    nu = area2(lightPos.y, lightPos.z, p1.y, p1.z, p2.y, p2.z);
+                                    nv = area2(lightPos.y, lightPos.z, p2.y, p2.z, p0.y, p0.z);
+                                    ood = 1.0f / mm.x;
+                                } else if (ay >= ax && ay >= az) {
+                                    nu = area2(lightPos.x, lightPos.z, p1.x, p1.z, p2.x, p2.z);
+                                    nv = area2(lightPos.x, lightPos.z, p2.x, p2.z, p0.x, p0.z);
+                                    ood = 1.0f / -mm.y;
+                                } else {
+                                    nu = area2(lightPos.x, lightPos.y, p1.x, p1.y, p2.x, p2.y);
+                                    nv = area2(lightPos.x, lightPos.y, p2.x, p2.y, p0.x, p0.y);
+                                    ood = 1.0f / mm.z;
+                                }
+                                const float bu = nu * ood, bv = nv * ood, bw = 1.0f - bu - bv;
+                                const float2 c0 = __ldg(&s.emisTc[3 * ei]), c1 = __ldg(&s.emisTc[3 * ei + 1]),
+                                             c2 = __ldg(&s.emisTc[3 * ei + 2]);
+                                const float2 etc = make_float2(bw * c0.x + bu * c1.x + bv * c2.x,
+                                                               bw * c0.y + bu * c1.y + bv * c2.y);
+                                const float4 tf = __ldg(&M.tf[3]);
+                                const float ex = etc.x * tf.z + tf.x, ey = etc.y * tf.w + tf.y;
+                                Le = Le * f3of4(sampleTexture(s.texels, __ldg(s.texInfo + __ldg(&EM.tex0).w), ex, ey));
+                            }
+                            const float cosX = fmaxf(0.0f, dot3(normal, ldir));
+                            const float G = cosX * cosY / (dist * dist);
+                            const float sxi = U.next();
+                            const float3 brdf = bsdf::evalBrdf(m, ldir, wo, U);
+                            const float3 colour = Le * brdf * G / (pdfA * selPdf);
+                            const float3 c = colour * T;
+                            if (nonzeroOrNonfinite(c)) {
+                                wantE = true;
+                                shE[0] = mk4(hitPoint, __int_as_float((int)path));
+                                shE[1] = mk4(ldir, dist - OPT_SCENE_EPSILON);
+                                shE[2] = mk4(c, sxi);
+                            }
+                        }
+                        if ((uint32_t)depth < fp.maxDepth) {
+                            // BSDF sampling, throughput, Russian roulette (cu/path_tracer.cu:522-581).
+                            float3 xi;
+                            xi.x = U.next();
+                            xi.y = U.next();
+                            xi.z = U.next();
+                            bsdf::Sample smp;
+                            smp.dir = mk3s(0.0f);
+                            smp.bsdf = mk3s(0.0f);
+                            smp.pdf = 0.0f;
+                            bsdf::sampleBrdf(m, wo, xi, U, smp);
+                            smp.pdf *= cw;
+                            if (!(smp.pdf < OPT_SCENE_EPSILON || maxc3(smp.bsdf) < OPT_SCENE_EPSILON)) {
+                                T = T * (smp.bsdf * fabsf(dot3(normal, smp.dir)) / smp.pdf);
+                                const float maxC = maxc3(T);
+                                bool alive = true;
+                                if (depth > 3 || maxC < 0.3f) {
+                                    const float qq = fmaxf(0.05f, 1.0f - maxC);
+                                    if (U.next() < qq)
+                                        alive = false;
+                                    else
+                                        T = T / (1.0f - qq);
+                                }
+                                if (alive) {
+                                    if (!spec)
+                                        hitPoint = hitPoint + rayDir * OPT_SHADOW_BIAS;
+                                    const float3 origin = hitPoint + smp.dir * OPT_SCENE_EPSILON;
+                                    cont = true;
+                                    nxtRay[0] = mk4(origin, __int_as_float((int)path));
+                                    nxtRay[1] = mk4(smp.dir, 0.0f);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            q.pathT[path] = mk4(T, __uint_as_float(flags));
+            q.pathL[path] = mk4(L, 0.0f);
+        }
+        warpPush<2>(cont, q.counters + CNT_EXT + depth + 1, nextQ, nxtRay);
+        warpPush<3>(wantP, q.counters + CNT_SHADOW_P + depth, shPQ, shP);
+        warpPush<3>(wantE, q.counters + CNT_SHADOW_E + depth, shEQ, shE);
+    }
+}
+
+// ------------------------------------------------------------------ shadow
+// Occlusion test of queued NEE rays, tmin = SCENE_EPSILON
+// (cu/path_tracer.cu:396,485, cu/device_programs.cu:180-219). An unoccluded
+// ray adds its contribution; an occluded one adds contribution * 0, which
+// only matters (as NaN) when the contribution was not finite, exactly as the
+// reference's lightVisibility product.
+template <bool COUNT>
+__global__ void __launch_bounds__(256) kShadow(DevScene s, FrameParams fp, WaveBufs q, int depth, int which)
+{
+    const uint32_t count = q.counters[(which == 0 ? CNT_SHADOW_P : CNT_SHADOW_E) + depth];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t sampleBase = __ldg(fp.state);
+    const uint32_t seed = __float_as_uint(__ldg(&fp.fc->eye).w);
+    typename std::conditional<COUNT, Count, NoCount>::type ctr;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
+        const float4 o = q.shO[which][j], d = q.shD[which][j], c = q.shC[which][j];
+        const uint32_t path = (uint32_t)__float_as_int(o.w);
+        const AlphaTest at = makeAlpha(s, seed, path % fp.npix, sampleBase + path / fp.npix, (uint32_t)depth, c.w);
+        HitRec h;
+        const bool occluded =
+            traverse<true>(s.nodes, s.triV, f3of4(o), f3of4(d), OPT_SCENE_EPSILON, d.w, h, at, ctr);
+        const float3 cc = f3of4(c);
+        const bool finite = isfinite(cc.x) && isfinite(cc.y) && isfinite(cc.z);
+        if (!occluded || !finite) {
+            float4 L = q.pathL[path];
+            const float3 add = occluded ? cc * 0.0f : cc;
+            q.pathL[path] = make_float4(L.x + add.x, L.y + add.y, L.z + add.z, L.w);
+        }
+    }
+    if constexpr (COUNT)
+        flushCounts(ctr, q.totals, 6);
+}
+
+// ------------------------------------------------------------------ accumulate
+// FP64 progressive accumulation, then tone mapping and gamma
+// (cu/device_programs.cu:67-101, include/tone_mapping.h:5-29,
+// include/gamma_correction.h:3-7). A NaN sample contributes the running mean,
+// which is what the reference's lerp does when it skips the write.
+__global__ void __launch_bounds__(256) kAccumulate(FrameParams fp, WaveBufs q, AccumBufs a)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t samplesBefore = __ldg(fp.state);
+    const int toneFlags = __float_as_int(__ldg(&fp.fc->V).w);
+    const float gammaTerm = __ldg(&fp.fc->W).w;
+    uint32_t nanLocal = 0;
+    for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < fp.npix; px += stride) {
+        Acc4 S = a.sum[px], Q = a.sumSq[px];
+        uint32_t n = samplesBefore;
+        for (uint32_t b = 0; b < fp.sppBatch; ++b) {
+            const float4 Lf = q.pathL[b * fp.npix + px];
+            double lx, ly, lz;
+            if (isnan(Lf.x) || isnan(Lf.y) || isnan(Lf.z)) {
+                ++nanLocal;
+                lx = n ? S.x / n : 0.0;
+                ly = n ? S.y / n : 0.0;
+                lz = n ? S.z / n : 0.0;
+            } else {
+                lx = Lf.x;
+                ly = Lf.y;
+                lz = Lf.z;
+            }
+            S.x += lx; S.y += ly; S.z += lz;
+            Q.x += lx * lx; Q.y += ly * ly; Q.z += lz * lz;
+            ++n;
+        }
+        a.sum[px] = S;
+        a.sumSq[px] = Q;
+        const double inv = 1.0 / (double)n;
+        float4 c = make_float4((float)(S.x * inv), (float)(S.y * inv), (float)(S.z * inv), 0.0f);
+        a.accumFrameBuffer[px] = c;
+        if (toneFlags & 1) {
+            if (!(toneFlags & 2)) {
+                c = make_float4(c.x / (c.x + 1.0f), c.y / (c.y + 1.0f), c.z / (c.z + 1.0f), c.w / (c.w + 1.0f));
+            } else {
+                auto aces = [](float x) {
+                    const float t = (x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f);
+                    return fmaxf(0.0f, fminf(t, 1.0f));
+                };
+                c = make_float4(aces(c.x), aces(c.y), aces(c.z), aces(c.w));
+            }
+        }
+        if (toneFlags & 4) {
+            const float ig = 1.0f / gammaTerm;
+            c = make_float4(powf(c.x, ig), powf(c.y, ig), powf(c.z, ig), c.w);
+        }
+        a.frameBuffer[px] = c;
+    }
+    // Per-frame statistics: NaN samples, and the ray counts of every queue.
+    for (int off = 16; off > 0; off >>= 1)
+        nanLocal += __shfl_down_sync(0xffffffffu, nanLocal, off);
+    if ((threadIdx.x & 31) == 0 && nanLocal)
+        atomicAdd(q.totals + 3, (unsigned long long)nanLocal);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        unsigned long long ext = 0, sh = 0;
+        for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
+            ext += q.counters[CNT_EXT + d];
+            sh += q.counters[CNT_SHADOW_P + d] + q.counters[CNT_SHADOW_E + d];
+        }
+        q.totals[0] += ext;
+        q.totals[1] += sh;
+        q.totals[2] += fp.numPaths;
+    }
+}
+
+// Advances the sample counter after a pass (one thread).
+__global__ void kAdvance(uint32_t *state, uint32_t by) { state[0] += by; }
+
+// ------------------------------------------------------------------ parity entry points
+__global__ void kTrace(DevScene s, const float4 *rays, float4 *hits, uint32_t n, int anyHit)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const float4 o = rays[2 * i], d = rays[2 * i + 1];
+    const AlphaTest at = makeAlpha(s, 0u, 0u, 0u, 0u, anyHit ? 0.5f : -1.0f);
+    HitRec h;
+    const bool hit = anyHit ? traverse<true>(s.nodes, s.triV, f3of4(o), f3of4(d), o.w, d.w, h, at)
+                            : traverse<false>(s.nodes, s.triV, f3of4(o), f3of4(d), o.w, d.w, h, at);
+    const int prim = hit ? __float_as_int(__ldg(&s.triV[3 * h.leaf]).w) : -1;
+    hits[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(prim))
+                  : make_float4(__int_as_float(0x7f800000), 0.0f, 0.0f, __int_as_float(-1));
+}
+
+// Layouts of optpt_bsdf_query / optpt_bsdf_result (include/optpt.h).
+struct BsdfQueryD {
+    float baseColour[3], emission[3], sheenColour[3];
+    float metallic, roughness, specular, transmissionWeight, subsurfaceWeight, coatWeight, coatRoughness,
+        sheenRoughnessMat, sheenRoughness, ior;
+    uint32_t category;
+    float n[3], wo[3], wi[3], xs[12];
+};
+struct BsdfResultD {
+    uint32_t category;
+    int32_t ret, used;
+    float categoryWeight;
+    float f[3], dir[3], bsdf[3];
+    float pdf;
+};
+struct XsSource {
+    const float *xs;
+    int used;
+    OPT_D float next()
+    {
+        const float x = used < 12 ? xs[used] : 0.5f;
+        ++used;
+        return x;
+    }
+};
+
+__global__ void kBsdfBatch(const BsdfQueryD *qs, BsdfResultD *rs, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const BsdfQueryD &Q = qs[i];
+    XsSource U{Q.xs, 0};
+    const float3 nn = mk3(Q.n[0], Q.n[1], Q.n[2]), wo = mk3(Q.wo[0], Q.wo[1], Q.wo[2]),
+                 wi = mk3(Q.wi[0], Q.wi[1], Q.wi[2]);
+    const float3 albedo = mk3(Q.baseColour[0], Q.baseColour[1], Q.baseColour[2]);
+    const float3 sheen = mk3(Q.sheenColour[0], Q.sheenColour[1], Q.sheenColour[2]);
+    const bsdf::CatIn ci{Q.category, Q.coatWeight, Q.coatRoughness, Q.transmissionWeight, Q.specular,
+                         Q.subsurfaceWeight};
+    float cw;
+    const uint32_t cat = bsdf::categorise(ci, wo, nn, Q.roughness, Q.metallic,
+                                          mk3(Q.emission[0], Q.emission[1], Q.emission[2]), sheen, Q.sheenRoughness,
+                                          U, cw);
+    BsdfResultD R;
+    R.category = cat;
+    R.categoryWeight = cw;
+    if (cat & MF_EMISSION) {
+        for (int k = 0; k < 3; ++k)
+            R.f[k] = R.dir[k] = R.bsdf[k] = 0.0f;
+        R.pdf = 0.0f;
+        R.ret = 0;
+        R.used = U.used;
+        rs[i] = R;
+        return;
+    }
+    const bsdf::MatMR m = bsdf::makeMatMR(albedo, Q.ior, Q.metallic, sheen, cat, nn, Q.roughness, Q.coatRoughness,
+                                          Q.sheenRoughnessMat);
+    const float3 f = bsdf::evalBrdf(m, wi, wo, U);
+    float3 xi;
+    xi.x = U.next();
+    xi.y = U.next();
+    xi.z = U.next();
+    bsdf::Sample smp;
+    smp.dir = mk3s(0.0f);
+    smp.bsdf = mk3s(0.0f);
+    smp.pdf = 0.0f;
+    const bool ok = bsdf::sampleBrdf(m, wo, xi, U, smp);
+    smp.pdf *= cw;
+    R.f[0] = f.x; R.f[1] = f.y; R.f[2] = f.z;
+    R.dir[0] = smp.dir.x; R.dir[1] = smp.dir.y; R.dir[2] = smp.dir.z;
+    R.bsdf[0] = smp.bsdf.x; R.bsdf[1] = smp.bsdf.y; R.bsdf[2] = smp.bsdf.z;
+    R.pdf = smp.pdf;
+    R.ret = ok ? 1 : 0;
+    R.used = U.used;
+    rs[i] = R;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launchGenerate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs &q, cudaStream_t st)
+{
+    kGenerate<<<ls.gridGenerate, ls.block, 0, st>>>(fp, q);
+}
+void launchExtend(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
+                  cudaStream_t st, bool count)
+{
+    if (count)
+        kExtend<true><<<ls.gridExtend, ls.block, 0, st>>>(s, fp, q, depth);
+    else
+        kExtend<false><<<ls.gridExtend, ls.block, 0, st>>>(s, fp, q, depth);
+}
+void launchShade(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
+                 cudaStream_t st)
+{
+    kShade<<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
+}
+void launchShadow(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
+                  int which, cudaStream_t st, bool count)
+{
+    if (count)
+        kShadow<true><<<ls.gridShadow, ls.block, 0, st>>>(s, fp, q, depth, which);
+    else
+        kShadow<false><<<ls.gridShadow, ls.block, 0, st>>>(s, fp, q, depth, which);
+}
+void launchAccumulate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs &q, const AccumBufs &a,
+                      cudaStream_t st)
+{
+    kAccumulate<<<ls.gridAccum, ls.block, 0, st>>>(fp, q, a);
+}
+void launchAdvance(const FrameParams &fp, uint32_t *state, cudaStream_t st)
+{
+    kAdvance<<<1, 1, 0, st>>>(state, fp.sppBatch);
+}
+void launchTrace(const DevScene &s, const float4 *rays, float4 *hits, uint32_t n, int anyHit, cudaStream_t st)
+{
+    if (n == 0)
+        return;
+    kTrace<<<(n + 127) / 128, 128, 0, st>>>(s, rays, hits, n, anyHit);
+}
+void launchBsdfBatch(const void *queries, void *results, uint32_t n, cudaStream_t st)
+{
+    if (n == 0)
+        return;
+    kBsdfBatch<<<(n + 127) / 128, 128, 0, st>>>(static_cast<const BsdfQueryD *>(queries),
+                                                 static_cast<BsdfResultD *>(results), n);
+}
+
+int occupancyGrid(int kernelId, int block)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const void *fn = nullptr;
+    switch (kernelId) {
+    case 0: fn = (const void *)kGenerate; break;
+    case 1: fn = (const void *)kExtend<false>; break;
+    case 2: fn = (const void *)kShade; break;
+    case 3: fn = (const void *)kShadow<false>; break;
+    default: fn = (const void *)kAccumulate; break;
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0);
+    if (per < 1)
+        per = 1;
+    return sms * per;
+}
+
+// sRGB decode table, IEC 61966-2-1.
+int uploadSrgbTable()
+{
+    float t[256];
+    for (int i = 0; i < 256; ++i) {
+        double c = i / 255.0;
+        t[i] = (float)(c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4));
+    }
+    return (int)cudaMemcpyToSymbol(c_srgbToLinear, t, sizeof(t));
+}

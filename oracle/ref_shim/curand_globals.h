@@ -1,0 +1,2 @@
+#pragma once
+// Intentionally empty: replaced by curand_kernel.h in this directory.

@@ -1,0 +1,111 @@
+"""Helpers for the GPU parity tests: device buffers through torch, seeded rays,
+and scene structs built from numpy arrays."""
+import ctypes
+
+import numpy as np
+
+
+def to_dev(arr, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(arr)).to(dev)
+
+
+def bsdf_on_gpu(q, dev):
+    import torch
+
+    import optix_pt_gb300 as opt
+    qb = np.ascontiguousarray(q).view(np.uint8)
+    qd = torch.from_numpy(qb.copy()).to(dev)
+    rd = torch.zeros(len(q) * opt.BSDF_RESULT.itemsize, dtype=torch.uint8, device=dev)
+    opt.bsdf_batch(qd.data_ptr(), rd.data_ptr(), len(q), torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    return rd.cpu().numpy().view(opt.BSDF_RESULT)
+
+
+def rays_towards(rng, n, origin_box, target_box, tmin=0.0, tmax=1e16):
+    o = rng.uniform(origin_box[0], origin_box[1], (n, 3))
+    t = rng.uniform(target_box[0], target_box[1], (n, 3))
+    d = t - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3] = o
+    r[:, 3] = tmin
+    r[:, 4:7] = d
+    r[:, 7] = tmax
+    return r
+
+
+def trace_on_gpu(renderer, rays, dev, any_hit=False):
+    import torch
+    rd = to_dev(rays, dev)
+    hd = torch.zeros((len(rays), 4), dtype=torch.float32, device=dev)
+    renderer.trace(rd.data_ptr(), hd.data_ptr(), len(rays), any_hit, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    return hd.cpu().numpy()
+
+
+class ArrayScene:
+    """An optpt_scene over numpy arrays (kept alive by this object)."""
+
+    def __init__(self, positions, tri_indices, mat_indices, materials, lights=(), normals=None, tex_coords=None,
+                 cam=((0, 0, 3), (0, 0, 0), (0, 1, 0), 40.0), res=(64, 64), bg=(0, 0, 0), max_depth=8):
+        from optix_pt_gb300 import _ffi
+        self.P = np.ascontiguousarray(positions, np.float32)
+        self.I = np.ascontiguousarray(tri_indices, np.int32)
+        self.M = np.ascontiguousarray(mat_indices, np.int32)
+        self.N = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        self.T = None if tex_coords is None else np.ascontiguousarray(tex_coords, np.float32)
+        self.mats = (_ffi.MaterialData * len(materials))(*materials)
+        self.lights = (_ffi.Light * max(1, len(lights)))(*lights)
+        s = _ffi.SceneStruct()
+        fp = ctypes.POINTER(ctypes.c_float)
+        ip = ctypes.POINTER(ctypes.c_int32)
+        s.positions = self.P.ctypes.data_as(fp)
+        s.numVertices = len(self.P)
+        s.normals = self.N.ctypes.data_as(fp) if self.N is not None else None
+        s.texCoords = self.T.ctypes.data_as(fp) if self.T is not None else None
+        s.triIndices = self.I.ctypes.data_as(ip)
+        s.numTriangles = len(self.I)
+        s.matIndices = self.M.ctypes.data_as(ip)
+        s.materials = ctypes.cast(self.mats, ctypes.POINTER(_ffi.MaterialData))
+        s.numMaterials = len(materials)
+        s.lights = ctypes.cast(self.lights, ctypes.POINTER(_ffi.Light))
+        s.numLights = len(lights)
+        s.camEye[:], s.camTarget[:], s.camUp[:] = cam[0], cam[1], cam[2]
+        s.camFovYDeg = cam[3]
+        s.resX, s.resY = res
+        s.bgColour[:] = bg
+        s.maxDepth = max_depth
+        self.struct = s
+        self.num_triangles = len(self.I)
+
+
+def material(rgb=(0.5, 0.5, 0.5), **kw):
+    from optix_pt_gb300 import _ffi
+    m = _ffi.MaterialData()
+    for name in ("baseColourTexture", "normalTexture", "metallicRoughnessTexture", "emissiveTexture",
+                 "sheenColourTexture", "sheenRoughnessTexture"):
+        setattr(m, name, -1)
+    for tf in ("baseColourTexTf", "normalTexTf", "metallicRoughnessTexTf", "emissiveTexTf", "sheenColourTexTf",
+               "sheenRoughnessTexTf"):
+        getattr(m, tf).scale[:] = [1.0, 1.0]
+    m.baseColour[:] = [rgb[0], rgb[1], rgb[2], 1.0]
+    m.alphaCutoff = 0.5
+    m.ior = 1.5
+    m.roughness = 1.0
+    for k, v in kw.items():
+        if k in ("emission", "sheenColour"):
+            getattr(m, k)[:] = v
+        else:
+            setattr(m, k, v)
+    return m
+
+
+def soup(n, seed, dup=False, scale=0.15):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-1, 1, (n, 3))
+    if dup:
+        c[n // 2:] = c[: n - n // 2]
+    P = (c[:, None, :] + rng.normal(scale=scale, size=(n, 3, 3))).reshape(-1, 3).astype(np.float32)
+    I = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+    return P, I

@@ -1,0 +1,151 @@
+"""GPU parity through the C ABI: device BSDF vs the reference's golden vectors
+and the FP64 oracle; Morton codes, leaf order and BVH topology bit-exact vs the
+host build; closest-hit and occlusion results bit-exact vs the host traversal."""
+import os
+
+import numpy as np
+import pytest
+
+from bsdf_cases import FP32_ENVELOPE, agreement, make_fixed_category_queries, make_queries, within
+from conftest import GOLDEN
+from gpu_util import ArrayScene, bsdf_on_gpu, material, rays_towards, soup, trace_on_gpu
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def test_bsdf_matches_reference_golden_vectors(cuda_dev):
+    g = np.load(os.path.join(GOLDEN, "bsdf_golden.npz"))
+    q, ref = g["queries"], g["results"]
+    res = bsdf_on_gpu(q, cuda_dev)
+    assert np.array_equal(res["category"], ref["category"])
+    assert np.array_equal(res["used"], ref["used"])
+    assert (res["ret"] == ref["ret"]).mean() > 0.999
+    # FP32 device vs FP32 host build of the reference: within the FP32 envelope
+    ok, bad = within(agreement(q, res, ref))
+    assert ok, bad
+    # and the category weight is computed exactly the same way
+    assert np.allclose(res["categoryWeight"], ref["categoryWeight"], rtol=1e-6)
+
+
+def test_bsdf_2pow24_queries_vs_fp64_oracle(cuda_dev):
+    """The material-sweep BSDF workload: 2^24 seeded queries on the GPU in 16
+    chunks; every 16th query is checked against the FP64 oracle, every query
+    for size-independent properties."""
+    checked = 0
+    agree_cat = 0
+    worst = {k: (0.0, 0.0) for k in FP32_ENVELOPE}
+    for chunk in range(16):
+        q = make_queries(1 << 20, 1000 + chunk) if chunk % 4 else make_fixed_category_queries(1 << 20, 1000 + chunk)
+        res = bsdf_on_gpu(q, cuda_dev)
+        assert (res["used"] <= 12).all()
+        pdf = res["pdf"]
+        assert (pdf[np.isfinite(pdf)] >= 0).all()
+        assert np.isfinite(res["dir"]).all(1).mean() > 0.999
+        sub = slice(chunk, None, 16)
+        qs = q[sub]
+        o64 = orc.bsdf_query(qs, precision=64)
+        agree_cat += int((res["category"][sub] == o64["category"]).sum())
+        checked += len(qs)
+        same = res["category"][sub] == o64["category"]
+        m = agreement(qs[same], res[sub][same], o64[same])
+        worst = {k: (max(worst[k][0], m[k][0]), max(worst[k][1], m[k][1])) for k in m}
+    assert agree_cat / checked > 0.9999
+    ok, bad = within(worst)
+    assert ok, bad
+
+
+def _scene_from(arrays_scene, leaf=4):
+    import optix_pt_gb300 as opt
+    return opt.Renderer(arrays_scene, leaf_size=leaf)
+
+
+def _scenes():
+    import optix_pt_gb300 as opt
+    out = [("cornell", opt.Scene.procedural("cornell")), ("spheres", opt.Scene.procedural("spheres"))]
+    for n, dup in ((1, False), (2, False), (5000, True), (20000, False)):
+        P, I = soup(n, 17 + n, dup)
+        out.append(("soup%d" % n, ArrayScene(P, I, np.zeros(n, np.int32), [material()])))
+    return out
+
+
+@pytest.mark.parametrize("leaf", [1, 4])
+def test_morton_codes_leaf_order_and_topology(cuda_dev, leaf):
+    for name, sc in _scenes():
+        r = _scene_from(sc, leaf)
+        v = orc.SceneView(sc.struct, leaf)
+        codes, order, nodes, used, leaves = v.bvh(sc.num_triangles)
+        gcodes, gorder = r.bvh_leaf_order()
+        assert np.array_equal(gcodes, codes), name
+        assert np.array_equal(gorder, order), name
+        gnodes = r.bvh_nodes()
+        assert np.array_equal(gnodes, nodes), name
+        st = r.stats()
+        assert (st["bvhNodes"], st["bvhLeaves"]) == (used, leaves), name
+        r.close()
+
+
+def test_closest_hit_bit_exact(cuda_dev):
+    rng = np.random.default_rng(7)
+    for name, sc in _scenes():
+        r = _scene_from(sc)
+        v = orc.SceneView(sc.struct, 4)
+        a = sc.arrays()["positions"] if hasattr(sc, "arrays") else sc.P
+        lo, hi = a.min(0), a.max(0)
+        pad = (hi - lo) * 0.3 + 1e-3
+        rays = rays_towards(rng, 1 << 16, (lo - pad, hi + pad), (lo, hi))
+        g = trace_on_gpu(r, rays, cuda_dev)
+        c = v.trace(rays)
+        assert np.array_equal(g.view(np.int32), c.view(np.int32)), \
+            "%s: %d of %d rays differ" % (name, int((g.view(np.int32) != c.view(np.int32)).any(1).sum()), len(rays))
+        assert (g[:, 3].view(np.int32) >= 0).mean() > 0.2, name
+        r.close()
+
+
+def test_occlusion_bit_exact(cuda_dev):
+    rng = np.random.default_rng(8)
+    for name, sc in _scenes()[:3]:
+        r = _scene_from(sc)
+        v = orc.SceneView(sc.struct, 4)
+        a = sc.arrays()["positions"] if hasattr(sc, "arrays") else sc.P
+        lo, hi = a.min(0), a.max(0)
+        rays = rays_towards(rng, 1 << 15, (lo, hi), (lo, hi), tmin=1e-4, tmax=1.0)
+        rays[:, 7] = rng.uniform(0.01, float(np.linalg.norm(hi - lo)), len(rays))
+        g = trace_on_gpu(r, rays, cuda_dev, any_hit=True)[:, 3].view(np.int32) >= 0
+        c = v.trace(rays, any_hit=True)[:, 3].view(np.int32) >= 0
+        assert np.array_equal(g, c), name
+        r.close()
+
+
+def test_alpha_mask_and_blend(cuda_dev):
+    """Alpha-tested candidates (cu/device_programs.cu:108-166): MASK ignores
+    alpha < cutoff, BLEND ignores xi > alpha; results equal the oracle's."""
+    n = 6000
+    P, I = soup(n, 99, scale=0.3)
+    mats = [material(), material(alphaMode=2, alphaCutoff=0.5), material(alphaMode=1)]
+    mats[1].baseColour[3] = 0.3   # masked out
+    mats[2].baseColour[3] = 0.5   # blended
+    M = (np.arange(n) % 3).astype(np.int32)
+    sc = ArrayScene(P, I, M, mats)
+    r = _scene_from(sc)
+    v = orc.SceneView(sc.struct, 4)
+    rng = np.random.default_rng(5)
+    rays = rays_towards(rng, 1 << 15, (-2, 2), (-1, 1))
+    for any_hit in (False, True):
+        g = trace_on_gpu(r, rays, cuda_dev, any_hit)
+        c = v.trace(rays, any_hit)
+        assert np.array_equal(g.view(np.int32), c.view(np.int32))
+        prims = g[:, 3].view(np.int32)
+        assert not np.isin(prims[prims >= 0] % 3, [1]).any()   # masked material never hit
+    r.close()
+
+
+def test_empty_and_tiny_scenes(cuda_dev):
+    P, I = soup(1, 3)
+    sc = ArrayScene(P, I, np.zeros(1, np.int32), [material()])
+    r = _scene_from(sc)
+    rays = rays_towards(np.random.default_rng(1), 256, (-2, 2), (-1, 1))
+    g = trace_on_gpu(r, rays, cuda_dev)
+    c = orc.SceneView(sc.struct, 4).trace(rays)
+    assert np.array_equal(g.view(np.int32), c.view(np.int32))
+    r.close()

@@ -1,0 +1,181 @@
+"""GPU renders vs the oracle integrator, and the Renderer surface.
+
+* Same random streams, same FP32 arithmetic: at 1 spp the GPU and the FP32
+  oracle follow the same path in almost every pixel.
+* Unbiasedness: GPU mean vs an independent FP64 oracle render, per-pixel z
+  test on the FP64 sums and sums of squares.
+"""
+import numpy as np
+import pytest
+
+from gpu_util import ArrayScene, material
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _camera(r):
+    lp = r.launch_params()
+    return list(lp.eye) + list(lp.U) + list(lp.V) + list(lp.W) + list(lp.bgColour), lp
+
+
+def _render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None, threads=None):
+    import torch
+
+    import optix_pt_gb300 as opt
+    r = opt.Renderer(scene, spp_batch=batch or 0)
+    r.setupOutputBuffer(w, h)
+    r.render(spp_gpu, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    s, q, n = r.accum()
+    cam, lp = _camera(r)
+    v = orc.SceneView(scene.struct, 4)
+    cs, cq, cnt = v.render(cam, w, h, lp.seed, cpu_base, spp_cpu, lp.maxDepth, precision=precision,
+                           threads=threads)
+    st = r.stats()
+    r.close()
+    return (s.reshape(-1, 3), q.reshape(-1, 3), n), (cs, cq, spp_cpu), st, cnt
+
+
+def _ztest(g, c):
+    (gs, gq, gn), (cs, cq, cn) = g, c
+    gm, cm = gs / gn, cs / cn
+    gv = np.maximum(gq / gn - gm ** 2, 0) / gn
+    cv = np.maximum(cq / cn - cm ** 2, 0) / cn
+    var = gv + cv
+    live = var > 0
+    z = np.zeros_like(gm)
+    z[live] = np.abs(gm - cm)[live] / np.sqrt(var[live])
+    # channels with zero variance on both sides must agree exactly-ish
+    dead_ok = np.all(np.abs(gm - cm)[~live] < 1e-6)
+    return z, live, dead_ok
+
+
+def test_cornell_one_sample_follows_oracle_paths(cuda_dev):
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    g, c, st, cnt = _render_pair(sc, 96, 96, 1, 1, 0, 32, batch=1)
+    gl, cl = g[0], c[0]
+    close = np.abs(gl - cl) <= 1e-4 * np.maximum(1.0, np.abs(cl)) + 1e-5
+    frac = close.all(1).mean()
+    assert frac > 0.97, frac
+    # the same rays were traced (up to the few diverged paths)
+    assert abs(int(st["extensionRays"]) - int(cnt[0])) <= 0.03 * int(cnt[0])
+
+
+def test_cornell_unbiased_against_fp64(cuda_dev):
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    g, c, st, cnt = _render_pair(sc, 96, 96, 256, 64, 10_000, 64)
+    z, live, dead_ok = _ztest(g, c)
+    assert dead_ok
+    frac = float((z[live] > 3.0).mean())
+    # expected two-sided 3-sigma rate is 0.27%; heavy-tailed radiance inflates it a little
+    assert frac < 0.01, frac
+    gm, cm = g[0] / g[2], c[0] / c[2]
+    assert abs(gm.mean() - cm.mean()) < 0.01 * cm.mean()
+
+
+def test_spheres_crop_unbiased_against_fp64(cuda_dev):
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("spheres")
+    g, c, st, cnt = _render_pair(sc, 160, 90, 64, 16, 20_000, 64)
+    z, live, dead_ok = _ztest(g, c)
+    frac = float((z[live] > 3.0).mean())
+    assert frac < 0.02, frac
+    gm, cm = g[0] / g[2], c[0] / c[2]
+    assert abs(gm.mean() - cm.mean()) < 0.02 * cm.mean()
+    assert st["shadowRays"] > 0 and st["extensionRays"] > 0
+
+
+def test_graph_and_direct_launch_are_identical(cuda_dev):
+    import torch
+
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    outs = []
+    for graph in (True, False):
+        r = opt.Renderer(sc, spp_batch=4, use_graph=graph)
+        r.setupOutputBuffer(64, 48)
+        r.render(10, torch.cuda.current_stream())   # 2 graph passes + a remainder of 2
+        torch.cuda.synchronize()
+        outs.append(r.accum())
+        assert r.getSampleCount() == 10
+        r.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_launch_and_framebuffer_match_tonemapped_mean(cuda_dev):
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    r = opt.Renderer(sc)
+    r.setupOutputBuffer(64, 64)
+    for _ in range(3):
+        r.launch()
+    assert r.getSampleCount() == 3
+    fb = r.getFrameBuffer()
+    s, q, n = r.accum()
+    mean = np.concatenate([s / n, np.zeros(s.shape[:2] + (1,))], -1).astype(np.float32).astype(np.float64)
+    expect = orc.tonemap(mean.reshape(-1, 4), tone=True, impl=1, gamma=True).reshape(fb.shape)
+    assert np.allclose(fb, expect, rtol=2e-5, atol=2e-6)
+    # Reinhard, gamma off
+    r.setToneMappingImpl(0)
+    r.setGammaCorrectionState(False)
+    r.launch()
+    fb = r.getFrameBuffer()
+    s, q, n = r.accum()
+    mean = np.concatenate([s / n, np.zeros(s.shape[:2] + (1,))], -1).astype(np.float32).astype(np.float64)
+    expect = orc.tonemap(mean.reshape(-1, 4), tone=True, impl=0, gamma=False).reshape(fb.shape)
+    assert np.allclose(fb, expect, rtol=2e-5, atol=2e-6)
+    r.resetSampleCount()
+    assert r.getSampleCount() == 0
+    s, q, n = r.accum()
+    assert not s.any()
+    r.close()
+
+
+def test_visualisation_albedo(cuda_dev):
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    r = opt.Renderer(sc)
+    r.setupOutputBuffer(32, 32)
+    r.setVis(7)
+    assert r.getVis() == 7
+    r.setToneMappingState(False)
+    r.setGammaCorrectionState(False)
+    r.launch()
+    fb = r.getFrameBuffer()[..., :3]
+    albedos = np.array([[0.73] * 3, [0.65, 0.05, 0.05], [0.12, 0.45, 0.15], [0, 0, 0]], np.float32)
+    d = np.abs(fb.reshape(-1, 1, 3) - albedos[None]).max(-1).min(-1)
+    assert (d < 1e-6).mean() > 0.95
+    r.close()
+
+
+def test_empty_scene_shows_background(cuda_dev):
+    sc = ArrayScene(np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0), [material()], bg=(0.25, 0.5, 0.75))
+    import optix_pt_gb300 as opt
+    r = opt.Renderer(sc)
+    r.setToneMappingState(False)
+    r.setGammaCorrectionState(False)
+    r.launch()
+    fb = r.getFrameBuffer()
+    assert np.allclose(fb[..., :3], [0.25, 0.5, 0.75])
+    r.close()
+
+
+def test_api_errors(cuda_dev):
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    r = opt.Renderer(sc)
+    lp = r.launch_params()
+    lp.maxDepth = 0
+    with pytest.raises(opt.OptptError):
+        r.updateLaunchParams(lp)
+    with pytest.raises(opt.OptptError):
+        r.setupOutputBuffer(0, 10)
+    with pytest.raises(opt.OptptError):
+        r.setupCamera((0, 0, 0), (0, 0, 1), (0, 1, 0), 0.0)
+    bad = ArrayScene(np.zeros((3, 3)), np.array([[0, 1, 5]]), np.zeros(1), [material()])
+    with pytest.raises(opt.OptptError):
+        opt.Renderer(bad)
+    r.close()

@@ -1,0 +1,124 @@
+"""Host LBVH and traversal of the oracle (CPU only): structural invariants and
+closest hits equal to a brute-force scan."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+
+def _tri_soup(n, seed, dup=False):
+    """A scene struct of n random triangles (optionally with duplicates, which
+    give equal Morton codes and exercise the index tie-break)."""
+    import ctypes
+
+    import optix_pt_gb300 as opt
+    from optix_pt_gb300 import _ffi
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-1, 1, (n, 3))
+    if dup:
+        c[n // 2:] = c[: n - n // 2]
+    P = (c[:, None, :] + rng.normal(scale=0.15, size=(n, 3, 3))).reshape(-1, 3).astype(np.float32)
+    I = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+    M = np.zeros(n, np.int32)
+    keep = [P, I, M]
+    mats = (_ffi.MaterialData * 1)()
+    mats[0].baseColour[:] = [0.5, 0.5, 0.5, 1.0]
+    for k in range(6):
+        setattr(mats[0], ["baseColourTexture", "normalTexture", "metallicRoughnessTexture", "emissiveTexture",
+                          "sheenColourTexture", "sheenRoughnessTexture"][k], -1)
+    s = _ffi.SceneStruct()
+    s.positions = P.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    s.numVertices = 3 * n
+    s.triIndices = I.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    s.numTriangles = n
+    s.matIndices = M.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    s.materials = ctypes.cast(mats, ctypes.POINTER(_ffi.MaterialData))
+    s.numMaterials = 1
+    keep.append(mats)
+    del opt
+    return s, keep, P.reshape(n, 3, 3)
+
+
+@pytest.mark.parametrize("n,dup,leaf", [(1, False, 4), (2, False, 1), (37, False, 4), (1000, True, 4),
+                                        (5000, False, 1), (5000, False, 8)])
+def test_lbvh_invariants(built, n, dup, leaf):
+    s, keep, tris = _tri_soup(n, 5, dup)
+    v = orc.SceneView(s, leaf)
+    codes, order, nodes, used, leaves = v.bvh(n)
+    assert (np.diff(codes.astype(np.int64)) >= 0).all()
+    assert np.array_equal(np.sort(order), np.arange(n))
+    # stable sort: equal codes keep primitive order
+    eq = np.diff(codes.astype(np.int64)) == 0
+    assert (np.diff(order)[eq] > 0).all()
+    # walk the tree: leaves partition [0, n) and respect the leaf size
+    covered = np.zeros(n, np.int32)
+    stack = [0]
+    seen = 0
+    while stack:
+        x = stack.pop()
+        seen += 1
+        for side in (0, 1):
+            ref, cnt = nodes[x, side], nodes[x, 2 + side]
+            if ref < 0:
+                continue
+            if cnt > 0:
+                assert cnt <= max(leaf, 1) or (x == 0 and n <= leaf)
+                covered[ref:ref + cnt] += 1
+            else:
+                stack.append(ref)
+    assert (covered == 1).all()
+    assert seen == used
+
+
+def test_traversal_equals_brute_force(built):
+    n = 1000
+    s, keep, tris = _tri_soup(n, 9)
+    v = orc.SceneView(s, 4)
+    rng = np.random.default_rng(1)
+    m = 1000
+    rays = np.zeros((m, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-1.5, 1.5, (m, 3))
+    d = rng.uniform(-0.5, 0.5, (m, 3)) - rays[:, 0:3]  # towards the cloud
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 7] = 1e16
+    hits = v.trace(rays)
+    prim = hits[:, 3].view(np.int32)
+    # brute force in float64 for the nearest t; compare IDs where the nearest
+    # two candidates are separated (ties are decided by the FP32 test itself)
+    o, dd = rays[:, None, 0:3].astype(np.float64), rays[:, None, 4:7].astype(np.float64)
+    a, b, c = (tris[None, :, k, :].astype(np.float64) for k in range(3))
+    e1, e2 = b - a, c - a
+    pv = np.cross(dd, e2)
+    det = np.einsum("ijk,ijk->ij", e1, pv)
+    inv = 1.0 / np.where(np.abs(det) < 1e-300, 1e-300, det)
+    tv = o - a
+    u = np.einsum("ijk,ijk->ij", tv, pv) * inv
+    qv = np.cross(tv, e1)
+    vv = np.einsum("ijk,ijk->ij", dd, qv) * inv
+    t = np.einsum("ijk,ijk->ij", e2, qv) * inv
+    ok = (u >= 0) & (vv >= 0) & (u + vv <= 1) & (t > 0)
+    t = np.where(ok, t, np.inf)
+    best = np.argmin(t, axis=1)
+    tbest = t[np.arange(m), best]
+    srt = np.sort(t, axis=1)
+    separated = (srt[:, 1] - srt[:, 0]) > 1e-4 * np.maximum(1, srt[:, 0])
+    expect = np.where(np.isfinite(tbest), best, -1)
+    mask = separated | ~np.isfinite(tbest)
+    assert (prim[mask] == expect[mask]).mean() > 0.999
+    assert np.isfinite(tbest).sum() > 200
+
+
+def test_any_hit_agrees_with_closest(built):
+    s, keep, tris = _tri_soup(2000, 13)
+    v = orc.SceneView(s, 4)
+    rng = np.random.default_rng(2)
+    m = 2000
+    rays = np.zeros((m, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-1.5, 1.5, (m, 3))
+    d = rng.normal(size=(m, 3))
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 3] = 1e-4
+    rays[:, 7] = rng.uniform(0.1, 3.0, m)
+    closest = v.trace(rays)[:, 3].view(np.int32) >= 0
+    anyhit = v.trace(rays, any_hit=True)[:, 3].view(np.int32) >= 0
+    assert np.array_equal(closest, anyhit)
