@@ -1,9 +1,10 @@
 """GPU renders vs the oracle integrator, and the Renderer surface.
 
-* Same random streams, same FP32 arithmetic: at 1 spp the GPU and the FP32
-  oracle follow the same path in almost every pixel.
-* Unbiasedness: GPU mean vs an independent FP64 oracle render, per-pixel z
-  test on the FP64 sums and sums of squares.
+* Paired: with the same random streams and FP32 arithmetic, the GPU and the
+  FP32 oracle follow the same path in almost every pixel.
+* Unbiasedness: a high-spp GPU render against an independent FP64 oracle
+  render (different sample indices): per-pixel z test on the FP64 sums and
+  sums of squares, and the frame mean within 4 standard errors.
 """
 import numpy as np
 import pytest
@@ -19,7 +20,7 @@ def _camera(r):
     return list(lp.eye) + list(lp.U) + list(lp.V) + list(lp.W) + list(lp.bgColour), lp
 
 
-def _render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None, threads=None):
+def _render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None):
     import torch
 
     import optix_pt_gb300 as opt
@@ -30,14 +31,13 @@ def _render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None,
     s, q, n = r.accum()
     cam, lp = _camera(r)
     v = orc.SceneView(scene.struct, 4)
-    cs, cq, cnt = v.render(cam, w, h, lp.seed, cpu_base, spp_cpu, lp.maxDepth, precision=precision,
-                           threads=threads)
+    cs, cq, cnt = v.render(cam, w, h, lp.seed, cpu_base, spp_cpu, lp.maxDepth, precision=precision)
     st = r.stats()
     r.close()
     return (s.reshape(-1, 3), q.reshape(-1, 3), n), (cs, cq, spp_cpu), st, cnt
 
 
-def _ztest(g, c):
+def _stats(g, c):
     (gs, gq, gn), (cs, cq, cn) = g, c
     gm, cm = gs / gn, cs / cn
     gv = np.maximum(gq / gn - gm ** 2, 0) / gn
@@ -46,46 +46,38 @@ def _ztest(g, c):
     live = var > 0
     z = np.zeros_like(gm)
     z[live] = np.abs(gm - cm)[live] / np.sqrt(var[live])
-    # channels with zero variance on both sides must agree exactly-ish
-    dead_ok = np.all(np.abs(gm - cm)[~live] < 1e-6)
-    return z, live, dead_ok
+    frac = float((z[live] > 3.0).mean()) if live.any() else 0.0
+    # frame mean and its standard error
+    se = np.sqrt(var.sum()) / var.size
+    return frac, abs(gm.mean() - cm.mean()), se, gm, cm, live
 
 
-def test_cornell_one_sample_follows_oracle_paths(cuda_dev):
+@pytest.mark.parametrize("name,w,h,spp", [("cornell", 96, 96, 1), ("cornell", 96, 96, 4), ("spheres", 160, 90, 2)])
+def test_paired_samples_follow_oracle_paths(cuda_dev, name, w, h, spp):
     import optix_pt_gb300 as opt
-    sc = opt.Scene.procedural("cornell")
-    g, c, st, cnt = _render_pair(sc, 96, 96, 1, 1, 0, 32, batch=1)
+    sc = opt.Scene.procedural(name)
+    g, c, st, cnt = _render_pair(sc, w, h, spp, spp, 0, 32, batch=spp)
     gl, cl = g[0], c[0]
     close = np.abs(gl - cl) <= 1e-4 * np.maximum(1.0, np.abs(cl)) + 1e-5
     frac = close.all(1).mean()
     assert frac > 0.97, frac
-    # the same rays were traced (up to the few diverged paths)
-    assert abs(int(st["extensionRays"]) - int(cnt[0])) <= 0.03 * int(cnt[0])
+    assert abs(int(st["extensionRays"]) - int(cnt[0])) <= 0.02 * int(cnt[0])
+    assert abs(int(st["shadowRays"]) - int(cnt[1])) <= 0.02 * max(1, int(cnt[1]))
 
 
-def test_cornell_unbiased_against_fp64(cuda_dev):
+@pytest.mark.parametrize("name,w,h,spp_gpu,spp_cpu,max_frac", [("cornell", 96, 96, 1024, 256, 0.01),
+                                                                 ("spheres", 80, 45, 1024, 128, 0.015)])
+def test_unbiased_against_fp64(cuda_dev, name, w, h, spp_gpu, spp_cpu, max_frac):
     import optix_pt_gb300 as opt
-    sc = opt.Scene.procedural("cornell")
-    g, c, st, cnt = _render_pair(sc, 96, 96, 256, 64, 10_000, 64)
-    z, live, dead_ok = _ztest(g, c)
-    assert dead_ok
-    frac = float((z[live] > 3.0).mean())
-    # expected two-sided 3-sigma rate is 0.27%; heavy-tailed radiance inflates it a little
-    assert frac < 0.01, frac
-    gm, cm = g[0] / g[2], c[0] / c[2]
-    assert abs(gm.mean() - cm.mean()) < 0.01 * cm.mean()
-
-
-def test_spheres_crop_unbiased_against_fp64(cuda_dev):
-    import optix_pt_gb300 as opt
-    sc = opt.Scene.procedural("spheres")
-    g, c, st, cnt = _render_pair(sc, 160, 90, 64, 16, 20_000, 64)
-    z, live, dead_ok = _ztest(g, c)
-    frac = float((z[live] > 3.0).mean())
-    assert frac < 0.02, frac
-    gm, cm = g[0] / g[2], c[0] / c[2]
-    assert abs(gm.mean() - cm.mean()) < 0.02 * cm.mean()
-    assert st["shadowRays"] > 0 and st["extensionRays"] > 0
+    sc = opt.Scene.procedural(name)
+    g, c, st, cnt = _render_pair(sc, w, h, spp_gpu, spp_cpu, 1 << 20, 64)
+    frac, dmean, se, gm, cm, live = _stats(g, c)
+    # two-sided 3-sigma rate is 0.27% for Gaussian means; heavy-tailed
+    # radiance with estimated variances lifts it somewhat
+    assert frac < max_frac, frac
+    assert dmean < 4 * se, (dmean, se)
+    rel_mse = float(np.mean((gm - cm) ** 2 / (cm ** 2 + 1e-2)))
+    print("%s: z>3 fraction %.4f, mean diff %.3g (SE %.3g), relMSE %.3g" % (name, frac, dmean, se, rel_mse))
 
 
 def test_graph_and_direct_launch_are_identical(cuda_dev):
@@ -105,6 +97,25 @@ def test_graph_and_direct_launch_are_identical(cuda_dev):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+def test_camera_change_needs_no_recapture(cuda_dev):
+    """Camera and tone settings live in device memory: moving the camera
+    between renders changes the image without rebuilding the graph."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    r = opt.Renderer(sc, spp_batch=2)
+    r.setupOutputBuffer(48, 48)
+    r.render(2, torch.cuda.current_stream())
+    a = r.frame_buffer()
+    r.resetSampleCount()
+    r.setupCamera((0.5, 1.2, 3.0), (0, 1, 0), (0, 1, 0), 50.0)
+    r.render(2, torch.cuda.current_stream())
+    b = r.frame_buffer()
+    assert not np.allclose(a, b)
+    r.close()
+
+
 def test_launch_and_framebuffer_match_tonemapped_mean(cuda_dev):
     import optix_pt_gb300 as opt
     sc = opt.Scene.procedural("cornell")
@@ -118,7 +129,6 @@ def test_launch_and_framebuffer_match_tonemapped_mean(cuda_dev):
     mean = np.concatenate([s / n, np.zeros(s.shape[:2] + (1,))], -1).astype(np.float32).astype(np.float64)
     expect = orc.tonemap(mean.reshape(-1, 4), tone=True, impl=1, gamma=True).reshape(fb.shape)
     assert np.allclose(fb, expect, rtol=2e-5, atol=2e-6)
-    # Reinhard, gamma off
     r.setToneMappingImpl(0)
     r.setGammaCorrectionState(False)
     r.launch()
