@@ -259,11 +259,21 @@ def run_ours(args, rank, world, local_rank):
         "generate": 64.0 * 2 * w * h,
     }
     peak, peak_kind = _peaks()
-    achieved = per_kernel_bytes[dominant] / (kms[dominant] / 1e3) / 1e9
+    # average launch: algorithmic bytes per launch / average launch duration
+    nl = max(1, prof["launches"][dominant])
+    achieved = (per_kernel_bytes[dominant] / nl) / (kms[dominant] / nl / 1e3) / 1e9
+    # DRAM traffic of the dominant kernel from the committed ncu capture
+    # (profiles/traffic.json), scaled from the captured launch to this run's
+    # average launch by the rays it processes.
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "extend_traffic.json")
-    if dominant == "extend" and os.path.exists(tp):
-        traffic = json.load(open(tp)).get("bytes_per_launch_scaled")
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    kname = {"extend": "kExtend", "shadow": "kShadow", "shade": "kShade"}.get(dominant)
+    if kname and os.path.exists(tp):
+        rec = json.load(open(tp)).get(kname)
+        if rec:
+            rays_kernel = prof["extensionRays"] if dominant != "shadow" else prof["shadowRays"]
+            per_launch_rays = rays_kernel / max(1, prof["launches"][dominant])
+            traffic = rec["dram_bytes_per_launch"] / rec["rays_per_launch"] * per_launch_rays
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "bytes_per_ray": {"extension": bytes_ext, "shadow": bytes_sh},
@@ -300,10 +310,10 @@ def run_ours(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-spp", type=int, default=6)
+    ap.add_argument("--cpu-spp", type=int, default=36)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
