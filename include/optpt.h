@@ -206,6 +206,19 @@ typedef struct optpt_traversal_work {
 } optpt_traversal_work;
 int optpt_traversal_counts(optpt_renderer *r, uint32_t spp, void *stream, optpt_traversal_work *out);
 
+/* ------------------------------------------------------------------ error reduction */
+
+/* Relative MSE of a progressive image against a reference image, reduced on
+ * the GPU in FP64 (the error measure of the equal-time comparisons; the
+ * reference keeps no error metric): mean over pixels of the sum over rgb of
+ * (I - R)^2 / (R^2 + 1e-2), with I = sum / nSamples. `sum` and `ref` are
+ * device arrays of double4 per pixel (xyz used; an accumulation buffer from
+ * optpt_device_buffers and a reference mean image); the result, one double,
+ * is written to device memory `out`, ordered on `stream`. Per-tile partial
+ * sums (one double per 2048 pixels) are allocated stream-ordered per call. */
+int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
+                 void *stream);
+
 /* ------------------------------------------------------------------ parity entry points */
 
 /* Closest-hit (anyHit = 0) or occlusion (anyHit = 1) queries against the

@@ -288,6 +288,11 @@ class Renderer:
         return nodes[:cnt.value]
 
 
+def relmse(sum_ptr, n_samples, ref_ptr, num_pixels, out_ptr, stream=None):
+    """GPU FP64 relMSE of sum / n_samples against ref (double4 per pixel, device pointers)."""
+    check(lib.optpt_relmse(sum_ptr, n_samples, ref_ptr, num_pixels, out_ptr, _stream_handle(stream)))
+
+
 def bsdf_batch(queries_ptr, results_ptr, n, stream=None):
     """Device BSDF queries (optpt_bsdf_query -> optpt_bsdf_result), device pointers."""
     check(lib.optpt_bsdf_batch(queries_ptr, results_ptr, n, _stream_handle(stream)))

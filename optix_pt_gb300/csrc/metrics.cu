@@ -1,0 +1,100 @@
+// Error reductions on the GPU, in FP64: the relative MSE of a progressive
+// image against a reference image, the error measure of the equal-time
+// comparisons (relMSE = mean over pixels of sum over rgb of
+// (I - R)^2 / (R^2 + 1e-2)).
+//
+// Two kernels: each block reduces one tile of RELMSE_TILE pixels to a partial
+// sum (scratch, one double per tile), then one block adds the partials in a
+// fixed order, so the result is deterministic for a given image size.
+#include <cuda_runtime.h>
+#include <string>
+#include "../../include/optpt.h"
+#include "engine.h"
+
+extern "C" int optpt_internal_set_error(int code, const char *msg);
+
+namespace {
+
+constexpr int RELMSE_BLOCK = 256;
+constexpr int RELMSE_PER_THREAD = 8;
+constexpr uint32_t RELMSE_TILE = RELMSE_BLOCK * RELMSE_PER_THREAD;
+
+__device__ __forceinline__ double blockSum(double v)
+{
+    __shared__ double warpSums[RELMSE_BLOCK / 32];
+    for (int off = 16; off > 0; off >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0)
+        warpSums[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < RELMSE_BLOCK / 32 ? warpSums[threadIdx.x] : 0.0;
+        for (int off = 16; off > 0; off >>= 1)
+            t += __shfl_down_sync(0xffffffffu, t, off);
+    }
+    return t;
+}
+
+__global__ void __launch_bounds__(RELMSE_BLOCK)
+    kRelMseTiles(const Acc4 *__restrict__ sum, double invN, const Acc4 *__restrict__ ref, uint32_t n,
+                 double *__restrict__ partial)
+{
+    const uint32_t base = blockIdx.x * RELMSE_TILE;
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < RELMSE_PER_THREAD; ++k) {
+        const uint32_t i = base + (uint32_t)k * RELMSE_BLOCK + threadIdx.x;
+        if (i < n) {
+            const Acc4 s = sum[i], r = ref[i];
+            const double dx = s.x * invN - r.x, dy = s.y * invN - r.y, dz = s.z * invN - r.z;
+            acc += dx * dx / (r.x * r.x + 1e-2) + dy * dy / (r.y * r.y + 1e-2) + dz * dz / (r.z * r.z + 1e-2);
+        }
+    }
+    const double t = blockSum(acc);
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(RELMSE_BLOCK)
+    kRelMseFinal(const double *__restrict__ partial, uint32_t tiles, uint32_t n, double *__restrict__ out)
+{
+    double acc = 0.0;
+    for (uint32_t i = threadIdx.x; i < tiles; i += RELMSE_BLOCK)
+        acc += partial[i];
+    const double t = blockSum(acc);
+    if (threadIdx.x == 0)
+        out[0] = t / (double)n;
+}
+
+}  // namespace
+
+// Launches both kernels with caller-chosen scratch (tiles doubles).
+int relmseLaunch(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
+                 double *scratch, cudaStream_t st)
+{
+    const uint32_t tiles = (numPixels + RELMSE_TILE - 1) / RELMSE_TILE;
+    kRelMseTiles<<<tiles, RELMSE_BLOCK, 0, st>>>(reinterpret_cast<const Acc4 *>(sum), 1.0 / (double)nSamples,
+                                                 reinterpret_cast<const Acc4 *>(ref), numPixels, scratch);
+    kRelMseFinal<<<1, RELMSE_BLOCK, 0, st>>>(scratch, tiles, numPixels, out);
+    return (int)cudaGetLastError();
+}
+
+uint32_t relmseTiles(uint32_t numPixels) { return (numPixels + RELMSE_TILE - 1) / RELMSE_TILE; }
+
+extern "C" int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
+                            void *stream)
+{
+    if (!sum || !ref || !out || numPixels == 0 || nSamples == 0)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "optpt_relmse: NULL buffer or empty image");
+    cudaStream_t st = (cudaStream_t)stream;
+    double *scratch = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&scratch, sizeof(double) * relmseTiles(numPixels), st);
+    if (e != cudaSuccess)
+        return optpt_internal_set_error(OPTPT_ERR_NOMEM, (std::string("optpt_relmse scratch: ") + cudaGetErrorString(e)).c_str());
+    int rc = relmseLaunch(sum, nSamples, ref, numPixels, out, scratch, st);
+    cudaFreeAsync(scratch, st);
+    if (rc)
+        return optpt_internal_set_error(OPTPT_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
+    return OPTPT_OK;
+}
