@@ -93,7 +93,7 @@ typedef struct optpt_scene {
 int optpt_scene_procedural(const char *name, uint32_t seed, optpt_scene *out);
 void optpt_scene_release(optpt_scene *scene);
 
-/* Resolves a scene-selection list in the reference's configs/*.json format
+/* Resolves a scene-selection list in the reference's configs/<name>.json format
  * (src/scene_desc.cpp:118-153: {"scene": id, id: name}) and parses the named
  * scene file (src/scene_desc.cpp:50-116). A scene file names either
  * "gltf scene file" (not supported: returns OPTPT_ERR_INVALID) or

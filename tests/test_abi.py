@@ -85,6 +85,37 @@ def test_struct_layouts_match_c(built):
     assert _ffi.BSDF_RESULT.fields["pdf"][1] == c["optpt_bsdf_result.pdf"]
 
 
+CPP_DROPIN = r"""
+#include "optix_pt/renderer.hpp"
+#include <cstdio>
+int main(int argc, char **argv) {
+    optix_pt::SceneDesc sd(argv[1]);
+    std::printf("%d %d %u\n", sd.resX, sd.resY, sd.scene.numTriangles);
+    try { optix_pt::SceneDesc bad("/nonexistent/list.json"); return 2; }
+    catch (const std::runtime_error &) { std::printf("caught\n"); }
+    return 0;
+}
+"""
+
+
+def test_cpp_dropin_header_compiles_and_parses_configs(built):
+    """include/optix_pt/renderer.hpp: the reference-named C++ classes over the C ABI."""
+    from optix_pt_gb300 import _ffi
+    libdir = os.path.dirname(_ffi.LIB_PATH)
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "t.cpp"), os.path.join(d, "t")
+        open(src, "w").write(CPP_DROPIN)
+        p = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src, "-o",
+                            exe, "-L", libdir, "-loptpt", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+        if p.returncode != 0:
+            if "not found" in p.stderr and "g++" in p.stderr:
+                pytest.skip("no C++ compiler")
+            raise AssertionError(p.stderr)
+        out = subprocess.run([exe, os.path.join(ROOT, "configs", "scene_selection.json")], capture_output=True,
+                             text=True, check=True).stdout.split()
+    assert out[:3] == ["512", "512", "36"] and out[3] == "caught"
+
+
 def test_oracle_query_layout_matches_product(built):
     from optix_pt_gb300 import _ffi
     from oracle.abi import BSDF_QUERY
