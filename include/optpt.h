@@ -219,6 +219,20 @@ int optpt_traversal_counts(optpt_renderer *r, uint32_t spp, void *stream, optpt_
 int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
                  void *stream);
 
+/* optpt_relmse for callers that cannot allocate device memory when they call
+ * it: code running inside a CUDA stream capture, frame loops that forbid
+ * allocator calls, or hosts whose own pool owns the device memory. No
+ * counterpart in the reference. Same arguments and result; it calls no
+ * cudaMalloc, cudaFree or other allocating routine. The partial sums use a
+ * fixed 32 KiB array in the library's device memory, which every GPU that
+ * loads the library holds until exit; it limits images to 8,388,608 pixels
+ * (OPTPT_ERR_INVALID beyond that). The first call on a device looks up that
+ * array's address (with the device current), so make the first call before
+ * any stream capture. All calls share the array: calls that overlap on the
+ * GPU (different streams, no ordering) race and must be avoided. */
+int optpt_relmse_noalloc(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
+                         void *stream);
+
 /* ------------------------------------------------------------------ parity entry points */
 
 /* Closest-hit (anyHit = 0) or occlusion (anyHit = 1) queries against the

@@ -156,6 +156,7 @@ _sigs = {
     "optpt_render_profiled": (ctypes.c_int, [_H, ctypes.c_uint32, _P, ctypes.POINTER(KernelTimes)]),
     "optpt_traversal_counts": (ctypes.c_int, [_H, ctypes.c_uint32, _P, ctypes.POINTER(TraversalCounts)]),
     "optpt_relmse": (ctypes.c_int, [_P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, _P]),
+    "optpt_relmse_noalloc": (ctypes.c_int, [_P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, _P]),
     "optpt_trace": (ctypes.c_int, [_H, _P, _P, ctypes.c_uint32, ctypes.c_int, _P]),
     "optpt_bvh_leaf_order": (ctypes.c_int, [_H, _P, _P]),
     "optpt_bvh_nodes": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),

@@ -7,6 +7,7 @@
 // sum (scratch, one double per tile), then one block adds the partials in a
 // fixed order, so the result is deterministic for a given image size.
 #include <cuda_runtime.h>
+#include <mutex>
 #include <string>
 #include "../../include/optpt.h"
 #include "engine.h"
@@ -81,6 +82,73 @@ int relmseLaunch(const double *sum, uint32_t nSamples, const double *ref, uint32
 }
 
 uint32_t relmseTiles(uint32_t numPixels) { return (numPixels + RELMSE_TILE - 1) / RELMSE_TILE; }
+
+// ------------------------------------------------------------------ allocation-free variant
+//
+// For callers that must not allocate device memory at the point of the call:
+// code inside a CUDA stream capture (cudaMalloc is not allowed there, and a
+// stream-ordered allocation would become part of the graph), real-time frame
+// loops that forbid allocator calls, and hosts whose memory pool owns all
+// device memory. The partial sums live in a fixed array in the library's own
+// device memory instead. It holds RELMSE_NOALLOC_TILES tiles, so images of up
+// to RELMSE_NOALLOC_TILES * 2048 = 8,388,608 pixels (a 3840x2160 frame fits);
+// larger images are rejected. Every GPU that loads the library keeps these
+// 32 KiB until the process exits.
+constexpr uint32_t RELMSE_NOALLOC_TILES = 4096;
+static __device__ __align__(256) double g_relmseScratch[RELMSE_NOALLOC_TILES];
+
+namespace {
+constexpr int MAX_DEVICES = 64;
+std::mutex g_scratchMutex;
+double *g_scratchAddr[MAX_DEVICES] = {};  // device address of g_relmseScratch, per device
+
+// Looks up (once per device, with that device current) the device address of
+// the scratch array; host code cannot use the symbol itself as a pointer.
+int scratchAddress(double **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return optpt_internal_set_error(OPTPT_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= MAX_DEVICES)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_scratchMutex);
+    if (!g_scratchAddr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_relmseScratch);
+        if (e != cudaSuccess)
+            return optpt_internal_set_error(OPTPT_ERR_CUDA,
+                                            (std::string("scratch address: ") + cudaGetErrorString(e)).c_str());
+        g_scratchAddr[dev] = static_cast<double *>(p);
+    }
+    *out = g_scratchAddr[dev];
+    return OPTPT_OK;
+}
+}  // namespace
+
+extern "C" int optpt_relmse_noalloc(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels,
+                                    double *out, void *stream)
+{
+    if (!sum || !ref || !out || numPixels == 0 || nSamples == 0)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "optpt_relmse_noalloc: NULL buffer or empty image");
+    if (relmseTiles(numPixels) > RELMSE_NOALLOC_TILES)
+        return optpt_internal_set_error(
+            OPTPT_ERR_INVALID,
+            ("optpt_relmse_noalloc: " + std::to_string(numPixels) + " pixels exceed the maximum of " +
+             std::to_string((unsigned long long)RELMSE_NOALLOC_TILES * RELMSE_TILE) + "; use optpt_relmse")
+                .c_str());
+    double *scratch = nullptr;
+    int rc = scratchAddress(&scratch);
+    if (rc)
+        return rc;
+    // Every tile the final kernel reads is written by the first kernel of the
+    // same call, so no clearing is needed; calls that overlap on the GPU
+    // share the array and race.
+    rc = relmseLaunch(sum, nSamples, ref, numPixels, out, scratch, (cudaStream_t)stream);
+    if (rc)
+        return optpt_internal_set_error(OPTPT_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
+    return OPTPT_OK;
+}
 
 extern "C" int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
                             void *stream)
