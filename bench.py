@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 WORKLOAD = {"workload": "material sweep: 8x8 icospheres (subdiv 4) + ground, 327,684 tris, point light + quad emitter",
             "scene": "spheres", "width": 1920, "height": 1080, "max_depth": 12, "spp_per_step": 1}
 METRIC = "Mrays/s (extension + shadow rays traced), progressive path tracing, 1 spp per step"
-NODE_BYTES = 64      # one BVH2 node: two child boxes + refs
+NODE_BYTES = {8: 80, 2: 64}  # compressed BVH8 node, BVH2 node
 TRI_BYTES = 48       # one leaf-ordered triangle record (3 x float4)
 RAY_IO_BYTES = 48    # ray in (origin, dir, tmax, path id) + hit out (t, u, v, id)
 
@@ -166,7 +166,7 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream(dev)
     scene = opt.Scene.procedural(WORKLOAD["scene"])
-    r = opt.Renderer(scene)
+    r = opt.Renderer(scene, bvh_width=args.bvh_width, leaf_size=args.leaf_size, block_size=args.block_size)
     w, h = WORKLOAD["width"], WORKLOAD["height"]
     r.setupOutputBuffer(w, h)
     a = scene.arrays()
@@ -249,8 +249,9 @@ def run_ours(args, rank, world, local_rank):
     sh_rays = max(1, cnt["shadowRays"])
     nodes_ext, tris_ext = cnt["extensionNodes"] / ext_rays, cnt["extensionTris"] / ext_rays
     nodes_sh, tris_sh = cnt["shadowNodes"] / sh_rays, cnt["shadowTris"] / sh_rays
-    bytes_ext = RAY_IO_BYTES + nodes_ext * NODE_BYTES + tris_ext * TRI_BYTES
-    bytes_sh = RAY_IO_BYTES + 4 + nodes_sh * NODE_BYTES + tris_sh * TRI_BYTES
+    nb = NODE_BYTES[args.bvh_width]
+    bytes_ext = RAY_IO_BYTES + nodes_ext * nb + tris_ext * TRI_BYTES
+    bytes_sh = RAY_IO_BYTES + 4 + nodes_sh * nb + tris_sh * TRI_BYTES
     per_kernel_bytes = {
         "extend": bytes_ext * prof["extensionRays"],
         "shadow": bytes_sh * prof["shadowRays"],
@@ -270,7 +271,7 @@ def run_ours(args, rank, world, local_rank):
     kname = {"extend": "kExtend", "shadow": "kShadow", "shade": "kShade"}.get(dominant)
     if kname and os.path.exists(tp):
         rec = json.load(open(tp)).get(kname)
-        if rec:
+        if rec and rec.get("rays_per_launch"):
             rays_kernel = prof["extensionRays"] if dominant != "shadow" else prof["shadowRays"]
             per_launch_rays = rays_kernel / max(1, prof["launches"][dominant])
             traffic = rec["dram_bytes_per_launch"] / rec["rays_per_launch"] * per_launch_rays
@@ -315,6 +316,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-spp", type=int, default=36)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8])
+    ap.add_argument("--leaf-size", type=int, default=0)
+    ap.add_argument("--block-size", type=int, default=0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))

@@ -108,6 +108,7 @@ typedef struct optpt_options {
     uint32_t blockSize;  /* threads per block for the wavefront kernels (0 = auto)  */
     uint32_t leafSize;   /* maximum triangles per BVH leaf, 1..8 (0 = auto)          */
     uint32_t useGraph;   /* capture the bounce loop in a CUDA graph (default 1)      */
+    uint32_t bvhWidth;   /* 8: compressed 8-wide BVH (default), 2: the binary LBVH   */
 } optpt_options;
 
 /* Uploads the scene and builds the BVH on the GPU. Replaces the reference's
@@ -175,6 +176,8 @@ typedef struct optpt_stats {
     uint64_t nanSamples;     /* samples dropped for NaN radiance        */
     uint32_t bvhNodes;       /* BVH2 nodes in use                       */
     uint32_t bvhLeaves;
+    uint32_t bvh8Nodes;      /* nodes of the compressed 8-wide BVH (0 if not built) */
+    uint32_t bvhWidth;       /* BVH traversed: 8 or 2                                */
     uint32_t sppBatch;
     uint32_t blockSize;
 } optpt_stats;
@@ -247,6 +250,12 @@ int optpt_trace(optpt_renderer *r, const float *rays, float *hits, uint32_t n, i
 /* The sorted 30-bit Morton codes and the primitive order of the BVH leaves
  * (host copies of numTriangles entries each), and the leaf size used. */
 int optpt_bvh_leaf_order(optpt_renderer *r, uint32_t *mortonSorted, int32_t *primOrder);
+
+/* The compressed 8-wide BVH in host memory: `nodes` receives numNodes 80-byte
+ * records (layout: optix_pt_gb300/csrc/bvh8.cuh), `primOrder8` the primitive
+ * index of every triangle slot in BVH8 leaf order. Either may be NULL to
+ * query the count. */
+int optpt_bvh8_nodes(optpt_renderer *r, void *nodes, uint32_t capacity, uint32_t *numNodes, int32_t *primOrder8);
 
 /* BVH2 topology in host memory: per node (child0, child1, count0, count1),
  * where count > 0 marks a leaf covering primOrder[child .. child+count). */

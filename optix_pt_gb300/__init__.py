@@ -94,9 +94,9 @@ SceneDesc = Scene.from_config  # the reference constructs SceneDesc from the sce
 class Renderer:
     """The reference's Renderer (include/renderer.h:19-206) on the GB300 engine."""
 
-    def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True):
+    def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True, bvh_width=8):
         self.scene = scene
-        opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0)
+        opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0, bvh_width)
         h = ctypes.c_void_p()
         check(lib.optpt_create(ctypes.byref(scene.struct), ctypes.byref(opt), ctypes.byref(h)))
         self._h = h
@@ -279,6 +279,15 @@ class Renderer:
         order = np.zeros(n, np.int32)
         check(lib.optpt_bvh_leaf_order(self._h, codes.ctypes.data, order.ctypes.data))
         return codes, order
+
+    def bvh8_nodes(self):
+        """(nodes as (N, 80) uint8, primitive per BVH8 triangle slot)."""
+        cnt = ctypes.c_uint32()
+        check(lib.optpt_bvh8_nodes(self._h, None, 0, ctypes.byref(cnt), None))
+        nodes = np.zeros((max(cnt.value, 1), 80), np.uint8)
+        order = np.zeros(max(self.scene.num_triangles, 1), np.int32)
+        check(lib.optpt_bvh8_nodes(self._h, nodes.ctypes.data, cnt.value, ctypes.byref(cnt), order.ctypes.data))
+        return nodes[:cnt.value], order[:self.scene.num_triangles]
 
     def bvh_nodes(self):
         cnt = ctypes.c_uint32()

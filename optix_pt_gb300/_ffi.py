@@ -96,13 +96,14 @@ class SceneStruct(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32), ("leafSize", ctypes.c_uint32),
-                ("useGraph", ctypes.c_uint32)]
+                ("useGraph", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("extensionRays", ctypes.c_uint64), ("shadowRays", ctypes.c_uint64),
                 ("pathSamples", ctypes.c_uint64), ("nanSamples", ctypes.c_uint64), ("bvhNodes", ctypes.c_uint32),
-                ("bvhLeaves", ctypes.c_uint32), ("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32)]
+                ("bvhLeaves", ctypes.c_uint32), ("bvh8Nodes", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32),
+                ("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32)]
 
 
 class KernelTimes(ctypes.Structure):
@@ -160,6 +161,7 @@ _sigs = {
     "optpt_trace": (ctypes.c_int, [_H, _P, _P, ctypes.c_uint32, ctypes.c_int, _P]),
     "optpt_bvh_leaf_order": (ctypes.c_int, [_H, _P, _P]),
     "optpt_bvh_nodes": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
+    "optpt_bvh8_nodes": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), _P]),
     "optpt_bsdf_batch": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P]),
 }
 EXPORTS = tuple(_sigs)

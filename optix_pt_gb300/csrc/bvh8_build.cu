@@ -1,0 +1,303 @@
+// Collapse of the LBVH (BVH2) into the compressed 8-wide BVH of bvh8.cuh, on
+// the GPU, one tree level per step:
+//   1. every BVH2 node that becomes a BVH8 node opens its children greedily,
+//      always the internal child of largest surface area, until 8 entries or
+//      only leaves remain;
+//   2. exclusive prefix sums over the items' internal-child and triangle
+//      counts place each node's children and triangles (so the layout is
+//      deterministic and reproducible on the host);
+//   3. each node is quantised (per-axis power-of-two scale, 8-bit child
+//      boxes rounded outwards by one step), its children are put in the slots
+//      of their centroid octants, and its leaf triangles are copied next to
+//      each other in slot order.
+#include <cub/cub.cuh>
+#include "bvh8.cuh"
+#include "engine.h"
+
+namespace {
+
+struct Entry {
+    int ref;  // BVH2 node (cnt == 0) or first sorted triangle (cnt > 0)
+    int cnt;
+    float lo[3], hi[3];
+};
+
+OPT_D float surfaceArea(const Entry &e)
+{
+    const float dx = e.hi[0] - e.lo[0], dy = e.hi[1] - e.lo[1], dz = e.hi[2] - e.lo[2];
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dy), __fmul_rn(dy, dz)), __fmul_rn(dz, dx));
+}
+
+OPT_D void childOf(const BvhNode &N, int side, Entry &e)
+{
+    e.ref = side == 0 ? N.d.x : N.d.y;
+    e.cnt = side == 0 ? N.d.z : N.d.w;
+    if (side == 0) {
+        e.lo[0] = N.a.x; e.hi[0] = N.a.y; e.lo[1] = N.a.z; e.hi[1] = N.a.w; e.lo[2] = N.c.x; e.hi[2] = N.c.y;
+    } else {
+        e.lo[0] = N.b.x; e.hi[0] = N.b.y; e.lo[1] = N.b.z; e.hi[1] = N.b.w; e.lo[2] = N.c.z; e.hi[2] = N.c.w;
+    }
+}
+
+__global__ void kCollapseOpen(const BvhNode *__restrict__ n2, const int *__restrict__ items, int nItems,
+                              Entry *__restrict__ ent, int *__restrict__ nEnt, int *__restrict__ kInt,
+                              int *__restrict__ nTri)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nItems)
+        return;
+    Entry e[8];
+    int ne = 0;
+    const BvhNode N = n2[items[i]];
+    for (int side = 0; side < 2; ++side) {
+        Entry c;
+        childOf(N, side, c);
+        if (c.ref >= 0)
+            e[ne++] = c;
+    }
+    while (ne < 8) {
+        int best = -1;
+        float bestA = -1.0f;
+        for (int j = 0; j < ne; ++j) {
+            if (e[j].cnt != 0)
+                continue;
+            const float A = surfaceArea(e[j]);
+            if (A > bestA) {
+                bestA = A;
+                best = j;
+            }
+        }
+        if (best < 0)
+            break;
+        const BvhNode C = n2[e[best].ref];
+        Entry l, r;
+        childOf(C, 0, l);
+        childOf(C, 1, r);
+        e[best] = l;
+        e[ne++] = r;
+    }
+    int k = 0, t = 0;
+    for (int j = 0; j < ne; ++j) {
+        ent[8 * i + j] = e[j];
+        if (e[j].cnt == 0)
+            ++k;
+        else
+            t += e[j].cnt;
+    }
+    nEnt[i] = ne;
+    kInt[i] = k;
+    nTri[i] = t;
+}
+
+OPT_D int scaleExponent(double ext)  // smallest e with 253 * 2^e >= ext, in [-126, 127]
+{
+    if (!(ext > 0.0))
+        return -126;
+    int e = ilogb(ext) - 7;
+    while (ldexp(253.0, e) < ext)
+        ++e;
+    while (e > -126 && ldexp(253.0, e - 1) >= ext)
+        --e;
+    return max(-126, min(127, e));
+}
+
+__global__ void kCollapseEmit(const int *__restrict__ items, int nItems, const Entry *__restrict__ ent,
+                              const int *__restrict__ nEnt, const int *__restrict__ scanK,
+                              const int *__restrict__ scanT, int levelStart, int nextStart, int triStart,
+                              const float4 *__restrict__ triV2, Bvh8Node *__restrict__ out,
+                              int *__restrict__ nextItems, float4 *__restrict__ triV8, int cap, int numTris)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nItems || levelStart + i >= cap || nextStart + scanK[i + 1] > cap ||
+        triStart + scanT[i + 1] > numTris)
+        return;  // bounds guard; a valid BVH2 never trips it (checked on the host)
+    const int ne = nEnt[i];
+    Entry e[8];
+    float lo[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+    float hi[3] = {-__int_as_float(0x7f800000), -__int_as_float(0x7f800000), -__int_as_float(0x7f800000)};
+    for (int j = 0; j < ne; ++j) {
+        e[j] = ent[8 * i + j];
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], e[j].lo[k]);
+            hi[k] = fmaxf(hi[k], e[j].hi[k]);
+        }
+    }
+    // Slots: each entry goes to its centroid's octant relative to the node
+    // centre, or the free slot nearest to it in Hamming distance.
+    float cen[3];
+    for (int k = 0; k < 3; ++k)
+        cen[k] = __fmul_rn(__fadd_rn(lo[k], hi[k]), 0.5f);
+    int slotOf[8];
+    uint32_t used = 0;
+    for (int j = 0; j < ne; ++j) {
+        uint32_t code = 0;
+        for (int k = 0; k < 3; ++k)
+            if (__fmul_rn(__fadd_rn(e[j].lo[k], e[j].hi[k]), 0.5f) > cen[k])
+                code |= 1u << k;
+        int slot = -1;
+        if (!((used >> code) & 1u)) {
+            slot = (int)code;
+        } else {
+            int bestD = 99;
+            for (int s = 0; s < 8; ++s) {
+                if ((used >> s) & 1u)
+                    continue;
+                const int dd = __popc((uint32_t)s ^ code);
+                if (dd < bestD) {
+                    bestD = dd;
+                    slot = s;
+                }
+            }
+        }
+        used |= 1u << slot;
+        slotOf[j] = slot;
+    }
+    int ex[3];
+    for (int k = 0; k < 3; ++k)
+        ex[k] = scaleExponent((double)hi[k] - (double)lo[k]);
+    uint32_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0}, qlo[3][8], qhi[3][8];
+    int refAt[8];
+    for (int s = 0; s < 8; ++s) {
+        refAt[s] = -1;
+        for (int k = 0; k < 3; ++k)
+            qlo[k][s] = qhi[k][s] = 0u;
+    }
+    for (int j = 0; j < ne; ++j)
+        refAt[slotOf[j]] = j;
+    uint32_t imask = 0;
+    const int childBase = nextStart + scanK[i];
+    const int triBase = triStart + scanT[i];
+    int rank = 0, toff = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int j = refAt[s];
+        if (j < 0)
+            continue;
+        for (int k = 0; k < 3; ++k) {
+            const double inv = ldexp(1.0, -ex[k]);
+            double ql = floor(((double)e[j].lo[k] - (double)lo[k]) * inv);
+            double qh = ceil(((double)e[j].hi[k] - (double)lo[k]) * inv);
+            ql = ql > 0.0 ? ql - 1.0 : 0.0;
+            qh = fmin(qh + 1.0, 255.0);
+            qlo[k][s] = (uint32_t)ql;
+            qhi[k][s] = (uint32_t)qh;
+        }
+        if (e[j].cnt == 0) {
+            imask |= 1u << s;
+            meta[s] = 1u;
+            nextItems[scanK[i] + rank] = e[j].ref;
+            ++rank;
+        } else {
+            meta[s] = ((uint32_t)e[j].cnt << 5) | (uint32_t)toff;
+            for (int c = 0; c < e[j].cnt; ++c) {
+                const int src = e[j].ref + c, dst = triBase + toff + c;
+                triV8[3 * dst] = triV2[3 * src];
+                triV8[3 * dst + 1] = triV2[3 * src + 1];
+                triV8[3 * dst + 2] = triV2[3 * src + 2];
+            }
+            toff += e[j].cnt;
+        }
+    }
+    Bvh8Node N;
+    const uint32_t ew = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) | ((uint32_t)(ex[2] + 127) << 16) |
+                        (imask << 24);
+    N.a = make_float4(lo[0], lo[1], lo[2], __uint_as_float(ew));
+    N.b = make_uint4((uint32_t)childBase, (uint32_t)triBase, meta[0] | meta[1] << 8 | meta[2] << 16 | meta[3] << 24,
+                     meta[4] | meta[5] << 8 | meta[6] << 16 | meta[7] << 24);
+    uint4 *q[3] = {&N.qx, &N.qy, &N.qz};
+    for (int k = 0; k < 3; ++k) {
+        q[k]->x = qlo[k][0] | qlo[k][1] << 8 | qlo[k][2] << 16 | qlo[k][3] << 24;
+        q[k]->y = qlo[k][4] | qlo[k][5] << 8 | qlo[k][6] << 16 | qlo[k][7] << 24;
+        q[k]->z = qhi[k][0] | qhi[k][1] << 8 | qhi[k][2] << 16 | qhi[k][3] << 24;
+        q[k]->w = qhi[k][4] | qhi[k][5] << 8 | qhi[k][6] << 16 | qhi[k][7] << 24;
+    }
+    out[levelStart + i] = N;
+}
+
+}  // namespace
+
+// Collapses a built BVH2 (`in`) into in.nodes8 / in.triV8. Returns 0 or a CUDA
+// error code.
+int buildBvh8(BvhBuild &in, int numTris, cudaStream_t st)
+{
+    if (numTris <= 0 || in.nodes == nullptr)
+        return 0;
+    const int cap = in.numNodes > 0 ? in.numNodes : 1;
+    cudaError_t err = cudaSuccess;
+    int *items = nullptr, *nextItems = nullptr, *nEnt = nullptr, *kInt = nullptr, *nTri = nullptr;
+    int *scanK = nullptr, *scanT = nullptr;
+    Entry *ent = nullptr;
+    void *temp = nullptr;
+    size_t tempBytes = 0;
+    int nItems = 1, levelStart = 0, triStart = 0, levels = 0;
+    const int zero = 0;
+#define CK8(x)                                                                                                         \
+    do {                                                                                                               \
+        if ((err = (x)) != cudaSuccess)                                                                                \
+            goto done;                                                                                                 \
+    } while (0)
+    CK8(cudaMalloc(&in.nodes8, sizeof(Bvh8Node) * cap));
+    CK8(cudaMalloc(&in.triV8, sizeof(float4) * 3 * (size_t)numTris));
+    CK8(cudaMalloc(&items, sizeof(int) * cap));
+    CK8(cudaMalloc(&nextItems, sizeof(int) * cap));
+    CK8(cudaMalloc(&nEnt, sizeof(int) * cap));
+    CK8(cudaMalloc(&kInt, sizeof(int) * (cap + 1)));
+    CK8(cudaMalloc(&nTri, sizeof(int) * (cap + 1)));
+    CK8(cudaMalloc(&scanK, sizeof(int) * (cap + 1)));
+    CK8(cudaMalloc(&scanT, sizeof(int) * (cap + 1)));
+    CK8(cudaMalloc(&ent, sizeof(Entry) * 8 * (size_t)cap));
+    CK8(cub::DeviceScan::ExclusiveSum(nullptr, tempBytes, kInt, scanK, cap + 1, st));
+    CK8(cudaMalloc(&temp, tempBytes));
+    CK8(cudaMemcpyAsync(items, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    while (nItems > 0 && levels < 256) {
+        const int G = (nItems + 127) / 128;
+        kCollapseOpen<<<G, 128, 0, st>>>(in.nodes, items, nItems, ent, nEnt, kInt, nTri);
+        // one extra zero entry so the exclusive scan's last element is the total
+        CK8(cudaMemsetAsync(kInt + nItems, 0, sizeof(int), st));
+        CK8(cudaMemsetAsync(nTri + nItems, 0, sizeof(int), st));
+        size_t tb = tempBytes;
+        CK8(cub::DeviceScan::ExclusiveSum(temp, tb, kInt, scanK, nItems + 1, st));
+        CK8(cub::DeviceScan::ExclusiveSum(temp, tb, nTri, scanT, nItems + 1, st));
+        int totals[2];
+        CK8(cudaMemcpyAsync(&totals[0], scanK + nItems, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK8(cudaMemcpyAsync(&totals[1], scanT + nItems, sizeof(int), cudaMemcpyDeviceToHost, st));
+        const int nextStart = levelStart + nItems;
+        kCollapseEmit<<<G, 128, 0, st>>>(items, nItems, ent, nEnt, scanK, scanT, levelStart, nextStart, triStart,
+                                         in.triV, in.nodes8, nextItems, in.triV8, cap, numTris);
+        CK8(cudaGetLastError());
+        CK8(cudaStreamSynchronize(st));
+        if (nextStart + totals[0] > cap) {  // cannot happen for a valid BVH2
+            err = cudaErrorInvalidValue;
+            goto done;
+        }
+        levelStart = nextStart;
+        triStart += totals[1];
+        nItems = totals[0];
+        int *t = items;
+        items = nextItems;
+        nextItems = t;
+        ++levels;
+    }
+    in.numNodes8 = levelStart;
+    in.levels8 = levels;
+    if (triStart != numTris)
+        err = cudaErrorInvalidValue;
+done:
+#undef CK8
+    cudaFree(items);
+    cudaFree(nextItems);
+    cudaFree(nEnt);
+    cudaFree(kInt);
+    cudaFree(nTri);
+    cudaFree(scanK);
+    cudaFree(scanT);
+    cudaFree(ent);
+    cudaFree(temp);
+    if (err != cudaSuccess) {
+        cudaFree(in.nodes8);
+        cudaFree(in.triV8);
+        in.nodes8 = nullptr;
+        in.triV8 = nullptr;
+        return (int)err;
+    }
+    return 0;
+}

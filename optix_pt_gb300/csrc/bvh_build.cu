@@ -391,5 +391,7 @@ void freeBvh(BvhBuild &b)
     cudaFree(b.triV);
     cudaFree(b.mortonSorted);
     cudaFree(b.primOrder);
+    cudaFree(b.nodes8);
+    cudaFree(b.triV8);
     b = BvhBuild{};
 }

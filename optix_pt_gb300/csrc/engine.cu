@@ -252,9 +252,10 @@ int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
     const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 256;
     r->shape.block = blk;
     r->shape.gridGenerate = occupancyGrid(0, blk);
-    r->shape.gridExtend = occupancyGrid(1, blk);
+    const bool wide = r->bvh.nodes8 != nullptr;
+    r->shape.gridExtend = occupancyGrid(wide ? 1 : 11, blk);
     r->shape.gridShade = occupancyGrid(2, blk);
-    r->shape.gridShadow = occupancyGrid(3, blk);
+    r->shape.gridShadow = occupancyGrid(wide ? 3 : 13, blk);
     r->shape.gridAccum = occupancyGrid(4, blk);
     r->graphDirty = true;
     return OPTPT_OK;
@@ -438,10 +439,18 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         r->opt = *options;
     else
         r->opt.useGraph = 1;
+    if (r->opt.bvhWidth == 0)
+        r->opt.bvhWidth = 8;
+    if (r->opt.bvhWidth != 2 && r->opt.bvhWidth != 8) {
+        delete r;
+        return fail(OPTPT_ERR_INVALID, "bvhWidth must be 2 or 8");
+    }
     if (r->opt.leafSize == 0)
-        r->opt.leafSize = 4;
-    if (r->opt.leafSize > 8)
-        r->opt.leafSize = 8;
+        r->opt.leafSize = r->opt.bvhWidth == 8 ? 3 : 4;
+    // BVH8 leaves address up to 32 triangles per node with 5-bit offsets.
+    const uint32_t maxLeaf = r->opt.bvhWidth == 8 ? 4u : 8u;
+    if (r->opt.leafSize > maxLeaf)
+        r->opt.leafSize = maxLeaf;
     int rc = OPTPT_OK;
     cudaError_t e;
     do {
@@ -519,9 +528,14 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
             rc = cudaFail((cudaError_t)be, "BVH build");
             break;
         }
+        if (r->opt.bvhWidth == 8 && (be = buildBvh8(r->bvh, (int)nt, r->ownStream))) {
+            rc = cudaFail((cudaError_t)be, "BVH8 collapse");
+            break;
+        }
         DevScene &ds = r->scene;
         ds.nodes = r->bvh.nodes;
-        ds.triV = r->bvh.triV;
+        ds.nodes8 = r->bvh.nodes8;
+        ds.triV = r->bvh.nodes8 ? r->bvh.triV8 : r->bvh.triV;
         ds.triIndices = r->dTriIndices;
         ds.normals = r->dNormals;
         ds.texCoords = r->dTexCoords;
@@ -780,6 +794,8 @@ int optpt_get_stats(optpt_renderer *r, optpt_stats *out)
     out->nanSamples = t[3];
     out->bvhNodes = (uint32_t)r->bvh.usedNodes;
     out->bvhLeaves = (uint32_t)r->bvh.numLeaves;
+    out->bvh8Nodes = (uint32_t)r->bvh.numNodes8;
+    out->bvhWidth = r->bvh.nodes8 ? 8u : 2u;
     out->sppBatch = r->sppBatch;
     out->blockSize = (uint32_t)r->shape.block;
     return OPTPT_OK;
@@ -901,6 +917,28 @@ int optpt_bvh_leaf_order(optpt_renderer *r, uint32_t *mortonSorted, int32_t *pri
     if (primOrder)
         CUDA_OR_RETURN(cudaMemcpy(primOrder, r->bvh.primOrder, sizeof(int32_t) * r->numTris, cudaMemcpyDeviceToHost),
                        "leaf order");
+    return OPTPT_OK;
+}
+
+int optpt_bvh8_nodes(optpt_renderer *r, void *nodes, uint32_t capacity, uint32_t *numNodes, int32_t *primOrder8)
+{
+    if (!r || !numNodes)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    *numNodes = (uint32_t)r->bvh.numNodes8;
+    if (r->bvh.nodes8 == nullptr)
+        return OPTPT_OK;
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "bvh8");
+    if (nodes) {
+        if (capacity < (uint32_t)r->bvh.numNodes8)
+            return fail(OPTPT_ERR_INVALID, "capacity below the node count");
+        CUDA_OR_RETURN(cudaMemcpy(nodes, r->bvh.nodes8, 80ull * r->bvh.numNodes8, cudaMemcpyDeviceToHost), "bvh8");
+    }
+    if (primOrder8) {
+        std::vector<float4> tv(3 * (size_t)r->numTris);
+        CUDA_OR_RETURN(cudaMemcpy(tv.data(), r->bvh.triV8, sizeof(float4) * tv.size(), cudaMemcpyDeviceToHost), "bvh8");
+        for (int i = 0; i < r->numTris; ++i)
+            memcpy(&primOrder8[i], &tv[3 * i].w, 4);
+    }
     return OPTPT_OK;
 }
 

@@ -4,6 +4,8 @@
 #include <stdint.h>
 #include "bvh.cuh"
 
+struct Bvh8Node;  // bvh8.cuh
+
 // Material record used by the shading kernels (derived from MaterialData at
 // upload): 10 x 16 B, read with vector loads.
 struct DevMaterial {
@@ -28,8 +30,9 @@ struct DevLight {
 };
 
 struct DevScene {
-    const BvhNode *nodes;
-    const float4 *triV;  // 3 per triangle, leaf order
+    const BvhNode *nodes;   // BVH2 (used when nodes8 is null)
+    const Bvh8Node *nodes8; // compressed BVH8
+    const float4 *triV;  // 3 per triangle, leaf order of the BVH in use
     const int *triIndices;  // int3 per primitive (original order)
     const float *normals;   // float3 per vertex or null
     const float *texCoords; // float2 per vertex or null
@@ -120,16 +123,23 @@ void launchTrace(const DevScene &s, const float4 *rays, float4 *hits, uint32_t n
 void launchBsdfBatch(const void *queries, void *results, uint32_t n, cudaStream_t st);
 int occupancyGrid(int kernelId, int block);  // persistent grid for a kernel class
 
-// bvh_build.cu
+// bvh_build.cu, bvh8_build.cu
+struct Bvh8Node;
 struct BvhBuild {
     BvhNode *nodes;        // n - 1 slots (holes where subtrees collapsed to leaves)
-    float4 *triV;          // 3 * n
+    float4 *triV;          // 3 * n, BVH2 leaf (Morton) order
     uint32_t *mortonSorted;
     int *primOrder;
     int numNodes;          // slots allocated
     int usedNodes;         // internal nodes emitted
     int numLeaves;
+    Bvh8Node *nodes8;      // compressed 8-wide BVH (null until collapsed)
+    float4 *triV8;         // 3 * n, BVH8 leaf order
+    int numNodes8;
+    int levels8;
 };
+// Collapses the BVH2 of `b` into b.nodes8 / b.triV8 (leaf sizes <= 4).
+int buildBvh8(BvhBuild &b, int numTris, cudaStream_t st);
 // Builds the LBVH on `st`. positions/triIndices/matIndices are device arrays;
 // triFlags (device, per primitive) go to triV[3i+2].w. Returns 0 or a CUDA error.
 int buildBvh(const float *positions, const int *triIndices, const int *matIndices, const uint32_t *triFlags,

@@ -15,10 +15,15 @@ struct HitRec {
 
 OPT_D float safeInv(float d) { return 1.0f / (fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d)); }
 
+// Slab tests compare the entry distance with min(exit, current hit) widened
+// by 2^-19 relative (cf. Ize, "Robust BVH Ray Traversal", JCGT 2(2), 2013):
+// rounding in the box test never culls a box whose triangle the watertight
+// test would hit, and boxes holding a triangle at exactly the current hit
+// distance are still opened, so equal-t candidates reach the index tie-break
+// whatever the tree shape.
+#define BOX_WIDEN 1.0000019f
+
 // Slab test of one child box; returns the entry distance or +inf on a miss.
-// The exit distance is widened by 4e-7 relative (Ize, "Robust BVH Ray
-// Traversal", JCGT 2(2), 2013) so rounding never culls a box whose triangle
-// the watertight test would hit.
 OPT_D float boxEntry(float lox, float hix, float loy, float hiy, float loz, float hiz, float3 o, float3 inv,
                      float tmin, float tmax)
 {
@@ -26,8 +31,8 @@ OPT_D float boxEntry(float lox, float hix, float loy, float hiy, float loz, floa
     float y0 = (loy - o.y) * inv.y, y1 = (hiy - o.y) * inv.y;
     float z0 = (loz - o.z) * inv.z, z1 = (hiz - o.z) * inv.z;
     float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
-    float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1)) * 1.0000004f;
-    return tn <= fminf(tf, tmax) ? tn : __int_as_float(0x7f800000);
+    float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+    return tn <= fminf(tf, tmax) * BOX_WIDEN ? tn : __int_as_float(0x7f800000);
 }
 
 // Walks the BVH. ANY = true stops at the first accepted hit (occlusion).

@@ -14,6 +14,18 @@
 #include "engine.h"
 #include "texture.cuh"
 #include "trace.cuh"
+#include "bvh8.cuh"
+
+// Closest hit / occlusion through the BVH in use: the compressed 8-wide BVH
+// (WIDE) or the BVH2 it was collapsed from.
+template <bool ANY, bool WIDE, class A, class C>
+OPT_D bool traceScene(const DevScene &s, float3 o, float3 d, float tmin, float tmax, HitRec &h, A alpha, C &&ctr)
+{
+    if constexpr (WIDE)
+        return traverse8<ANY>(s.nodes8, s.triV, o, d, tmin, tmax, h, alpha, ctr);
+    else
+        return traverse<ANY>(s.nodes, s.triV, o, d, tmin, tmax, h, alpha, ctr);
+}
 
 
 
@@ -136,7 +148,7 @@ OPT_D void flushCounts(const Count &c, unsigned long long *totals, int slot)
     }
 }
 
-template <bool COUNT>
+template <bool COUNT, bool WIDE>
 __global__ void __launch_bounds__(256) kExtend(DevScene s, FrameParams fp, WaveBufs q, int depth)
 {
     const uint32_t count = q.counters[CNT_EXT + depth];
@@ -150,7 +162,7 @@ __global__ void __launch_bounds__(256) kExtend(DevScene s, FrameParams fp, WaveB
         const uint32_t path = (uint32_t)__float_as_int(ro.w);
         const AlphaTest at = makeAlpha(s, seed, path % fp.npix, sampleBase + path / fp.npix, (uint32_t)depth, -1.0f);
         HitRec h;
-        const bool hit = traverse<false>(s.nodes, s.triV, f3of4(ro), f3of4(rd), 0.0f, 1e16f, h, at, ctr);
+        const bool hit = traceScene<false, WIDE>(s, f3of4(ro), f3of4(rd), 0.0f, 1e16f, h, at, ctr);
         q.hit[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.leaf))
                        : make_float4(__int_as_float(0x7f800000), 0.0f, 0.0f, __int_as_float(-1));
     }
@@ -510,7 +522,7 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
 // ray adds its contribution; an occluded one adds contribution * 0, which
 // only matters (as NaN) when the contribution was not finite, exactly as the
 // reference's lightVisibility product.
-template <bool COUNT>
+template <bool COUNT, bool WIDE>
 __global__ void __launch_bounds__(256) kShadow(DevScene s, FrameParams fp, WaveBufs q, int depth, int which)
 {
     const uint32_t count = q.counters[(which == 0 ? CNT_SHADOW_P : CNT_SHADOW_E) + depth];
@@ -524,7 +536,7 @@ __global__ void __launch_bounds__(256) kShadow(DevScene s, FrameParams fp, WaveB
         const AlphaTest at = makeAlpha(s, seed, path % fp.npix, sampleBase + path / fp.npix, (uint32_t)depth, c.w);
         HitRec h;
         const bool occluded =
-            traverse<true>(s.nodes, s.triV, f3of4(o), f3of4(d), OPT_SCENE_EPSILON, d.w, h, at, ctr);
+            traceScene<true, WIDE>(s, f3of4(o), f3of4(d), OPT_SCENE_EPSILON, d.w, h, at, ctr);
         const float3 cc = f3of4(c);
         const bool finite = isfinite(cc.x) && isfinite(cc.y) && isfinite(cc.z);
         if (!occluded || !finite) {
@@ -620,8 +632,13 @@ __global__ void kTrace(DevScene s, const float4 *rays, float4 *hits, uint32_t n,
     const float4 o = rays[2 * i], d = rays[2 * i + 1];
     const AlphaTest at = makeAlpha(s, 0u, 0u, 0u, 0u, anyHit ? 0.5f : -1.0f);
     HitRec h;
-    const bool hit = anyHit ? traverse<true>(s.nodes, s.triV, f3of4(o), f3of4(d), o.w, d.w, h, at)
-                            : traverse<false>(s.nodes, s.triV, f3of4(o), f3of4(d), o.w, d.w, h, at);
+    bool hit;
+    if (s.nodes8)
+        hit = anyHit ? traceScene<true, true>(s, f3of4(o), f3of4(d), o.w, d.w, h, at, NoCount())
+                     : traceScene<false, true>(s, f3of4(o), f3of4(d), o.w, d.w, h, at, NoCount());
+    else
+        hit = anyHit ? traceScene<true, false>(s, f3of4(o), f3of4(d), o.w, d.w, h, at, NoCount())
+                     : traceScene<false, false>(s, f3of4(o), f3of4(d), o.w, d.w, h, at, NoCount());
     const int prim = hit ? __float_as_int(__ldg(&s.triV[3 * h.leaf]).w) : -1;
     hits[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(prim))
                   : make_float4(__int_as_float(0x7f800000), 0.0f, 0.0f, __int_as_float(-1));
@@ -714,10 +731,11 @@ void launchGenerate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs
 void launchExtend(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                   cudaStream_t st, bool count)
 {
+    const bool wide = s.nodes8 != nullptr;
     if (count)
-        kExtend<true><<<ls.gridExtend, ls.block, 0, st>>>(s, fp, q, depth);
+        (wide ? kExtend<true, true> : kExtend<true, false>)<<<ls.gridExtend, ls.block, 0, st>>>(s, fp, q, depth);
     else
-        kExtend<false><<<ls.gridExtend, ls.block, 0, st>>>(s, fp, q, depth);
+        (wide ? kExtend<false, true> : kExtend<false, false>)<<<ls.gridExtend, ls.block, 0, st>>>(s, fp, q, depth);
 }
 void launchShade(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                  cudaStream_t st)
@@ -727,10 +745,13 @@ void launchShade(const LaunchShape &ls, const DevScene &s, const FrameParams &fp
 void launchShadow(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                   int which, cudaStream_t st, bool count)
 {
+    const bool wide = s.nodes8 != nullptr;
     if (count)
-        kShadow<true><<<ls.gridShadow, ls.block, 0, st>>>(s, fp, q, depth, which);
+        (wide ? kShadow<true, true> : kShadow<true, false>)<<<ls.gridShadow, ls.block, 0, st>>>(s, fp, q, depth,
+                                                                                               which);
     else
-        kShadow<false><<<ls.gridShadow, ls.block, 0, st>>>(s, fp, q, depth, which);
+        (wide ? kShadow<false, true> : kShadow<false, false>)<<<ls.gridShadow, ls.block, 0, st>>>(s, fp, q, depth,
+                                                                                                 which);
 }
 void launchAccumulate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs &q, const AccumBufs &a,
                       cudaStream_t st)
@@ -763,9 +784,11 @@ int occupancyGrid(int kernelId, int block)
     const void *fn = nullptr;
     switch (kernelId) {
     case 0: fn = (const void *)kGenerate; break;
-    case 1: fn = (const void *)kExtend<false>; break;
+    case 1: fn = (const void *)kExtend<false, true>; break;
     case 2: fn = (const void *)kShade; break;
-    case 3: fn = (const void *)kShadow<false>; break;
+    case 3: fn = (const void *)kShadow<false, true>; break;
+    case 11: fn = (const void *)kExtend<false, false>; break;
+    case 13: fn = (const void *)kShadow<false, false>; break;
     default: fn = (const void *)kAccumulate; break;
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0);

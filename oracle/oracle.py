@@ -21,6 +21,7 @@ def lib():
         _lib.orc_scene_view.argtypes = [P, ctypes.c_int]
         _lib.orc_scene_view_free.argtypes = [P]
         _lib.orc_bvh.argtypes = [P, P, P, P, ctypes.c_uint32, P]
+        _lib.orc_bvh8.argtypes = [P, P, ctypes.c_uint32, P, P]
         _lib.orc_trace.argtypes = [P, P, P, ctypes.c_uint32, ctypes.c_int, ctypes.c_int]
         _lib.orc_render.argtypes = [P, P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
@@ -92,6 +93,16 @@ class SceneView:
                            counts.ctypes.data)
         assert rc == 0
         return codes, order, nodes[:counts[0]], int(counts[1]), int(counts[2])
+
+    def bvh8(self, n_tris):
+        """(nodes as a (N, 80) uint8 array, primitive per BVH8 triangle slot)."""
+        counts = np.zeros(4, np.uint32)
+        lib().orc_bvh8(self._h, None, 0, None, counts.ctypes.data)
+        nodes = np.zeros((max(int(counts[0]), 1), 80), np.uint8)
+        order = np.zeros(max(n_tris, 1), np.int32)
+        rc = lib().orc_bvh8(self._h, nodes.ctypes.data, int(counts[0]), order.ctypes.data, counts.ctypes.data)
+        assert rc == 0
+        return nodes[:counts[0]], order[:n_tris]
 
     def trace(self, rays, any_hit=False, threads=None):
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)

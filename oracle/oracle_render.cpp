@@ -346,6 +346,198 @@ void buildHostBvh(const float *P, const int *I, int n, int leafSize, HostBvh &h)
     }
 }
 
+// ------------------------------------------------------------------ BVH8 collapse
+// The product's collapse rules restated: level by level, each BVH2 node that
+// becomes a BVH8 node opens its internal child of largest surface area until
+// it has 8 entries or only leaves; children and triangles are placed by
+// prefix sums in item order; children take their centroid-octant slot (or the
+// nearest free one by Hamming distance); boxes are quantised outwards by one
+// step with a per-axis power-of-two scale computed in double.
+struct Node8 {
+    float p[3];
+    uint32_t ew;
+    uint32_t childBase, triBase, meta0, meta1;
+    uint32_t q[3][4];
+};
+static_assert(sizeof(Node8) == 80, "80-byte node");
+
+struct Entry8 {
+    int ref, cnt;
+    float lo[3], hi[3];
+};
+
+float sa8(const Entry8 &e)
+{
+    float dx = e.hi[0] - e.lo[0], dy = e.hi[1] - e.lo[1], dz = e.hi[2] - e.lo[2];
+    return (dx * dy + dy * dz) + dz * dx;
+}
+
+int scaleExp(double ext)
+{
+    if (!(ext > 0.0))
+        return -126;
+    int e = std::ilogb(ext) - 7;
+    while (std::ldexp(253.0, e) < ext)
+        ++e;
+    while (e > -126 && std::ldexp(253.0, e - 1) >= ext)
+        --e;
+    return std::max(-126, std::min(127, e));
+}
+
+void buildHostBvh8(const HostBvh &B, std::vector<Node8> &out, std::vector<int> &order8)
+{
+    out.clear();
+    order8.clear();
+    const int n = (int)B.tris.size();
+    if (n == 0)
+        return;
+    auto child = [&](int node, int side, Entry8 &e) {
+        e.ref = B.nodes4[4 * (size_t)node + side];
+        e.cnt = B.nodes4[4 * (size_t)node + 2 + side];
+        const Box &b = side == 0 ? B.nodeBoxL[node] : B.nodeBoxR[node];
+        for (int k = 0; k < 3; ++k) {
+            e.lo[k] = b.lo[k];
+            e.hi[k] = b.hi[k];
+        }
+    };
+    std::vector<int> items{0};
+    order8.assign(n, -1);
+    int triStart = 0;
+    while (!items.empty()) {
+        const int levelStart = (int)out.size();
+        std::vector<std::vector<Entry8>> ents(items.size());
+        std::vector<int> scanK(items.size() + 1, 0), scanT(items.size() + 1, 0);
+        for (size_t i = 0; i < items.size(); ++i) {
+            std::vector<Entry8> &e = ents[i];
+            for (int side = 0; side < 2; ++side) {
+                Entry8 c;
+                child(items[i], side, c);
+                if (c.ref >= 0)
+                    e.push_back(c);
+            }
+            while (e.size() < 8) {
+                int best = -1;
+                float bestA = -1.0f;
+                for (size_t j = 0; j < e.size(); ++j) {
+                    if (e[j].cnt != 0)
+                        continue;
+                    float A = sa8(e[j]);
+                    if (A > bestA) {
+                        bestA = A;
+                        best = (int)j;
+                    }
+                }
+                if (best < 0)
+                    break;
+                Entry8 l, r;
+                child(e[best].ref, 0, l);
+                child(e[best].ref, 1, r);
+                e[best] = l;
+                e.push_back(r);
+            }
+            int k = 0, t = 0;
+            for (auto &x : e) {
+                if (x.cnt == 0)
+                    ++k;
+                else
+                    t += x.cnt;
+            }
+            scanK[i + 1] = scanK[i] + k;
+            scanT[i + 1] = scanT[i] + t;
+        }
+        const int nextStart = levelStart + (int)items.size();
+        std::vector<int> next(scanK.back());
+        out.resize(nextStart);
+        for (size_t i = 0; i < items.size(); ++i) {
+            const std::vector<Entry8> &e = ents[i];
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (auto &x : e)
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = std::fmin(lo[k], x.lo[k]);
+                    hi[k] = std::fmax(hi[k], x.hi[k]);
+                }
+            float cen[3];
+            for (int k = 0; k < 3; ++k)
+                cen[k] = (lo[k] + hi[k]) * 0.5f;
+            int refAt[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+            uint32_t used = 0;
+            for (size_t j = 0; j < e.size(); ++j) {
+                uint32_t code = 0;
+                for (int k = 0; k < 3; ++k)
+                    if ((e[j].lo[k] + e[j].hi[k]) * 0.5f > cen[k])
+                        code |= 1u << k;
+                int slot = -1;
+                if (!((used >> code) & 1u)) {
+                    slot = (int)code;
+                } else {
+                    int bestD = 99;
+                    for (int s = 0; s < 8; ++s) {
+                        if ((used >> s) & 1u)
+                            continue;
+                        int dd = __builtin_popcount((unsigned)s ^ code);
+                        if (dd < bestD) {
+                            bestD = dd;
+                            slot = s;
+                        }
+                    }
+                }
+                used |= 1u << slot;
+                refAt[slot] = (int)j;
+            }
+            int ex[3];
+            for (int k = 0; k < 3; ++k)
+                ex[k] = scaleExp((double)hi[k] - (double)lo[k]);
+            uint32_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0}, ql[3][8] = {}, qh[3][8] = {};
+            uint32_t imask = 0;
+            const int childBase = nextStart + scanK[i], triBase = triStart + scanT[i];
+            int rank = 0, toff = 0;
+            for (int s = 0; s < 8; ++s) {
+                const int j = refAt[s];
+                if (j < 0)
+                    continue;
+                for (int k = 0; k < 3; ++k) {
+                    const double inv = std::ldexp(1.0, -ex[k]);
+                    double a = std::floor(((double)e[j].lo[k] - (double)lo[k]) * inv);
+                    double b = std::ceil(((double)e[j].hi[k] - (double)lo[k]) * inv);
+                    a = a > 0.0 ? a - 1.0 : 0.0;
+                    b = std::fmin(b + 1.0, 255.0);
+                    ql[k][s] = (uint32_t)a;
+                    qh[k][s] = (uint32_t)b;
+                }
+                if (e[j].cnt == 0) {
+                    imask |= 1u << s;
+                    meta[s] = 1u;
+                    next[scanK[i] + rank] = e[j].ref;
+                    ++rank;
+                } else {
+                    meta[s] = ((uint32_t)e[j].cnt << 5) | (uint32_t)toff;
+                    for (int c = 0; c < e[j].cnt; ++c)
+                        order8[triBase + toff + c] = B.tris[e[j].ref + c].prim;
+                    toff += e[j].cnt;
+                }
+            }
+            Node8 &N = out[levelStart + i];
+            N.p[0] = lo[0];
+            N.p[1] = lo[1];
+            N.p[2] = lo[2];
+            N.ew = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) | ((uint32_t)(ex[2] + 127) << 16) |
+                   (imask << 24);
+            N.childBase = (uint32_t)childBase;
+            N.triBase = (uint32_t)triBase;
+            N.meta0 = meta[0] | meta[1] << 8 | meta[2] << 16 | meta[3] << 24;
+            N.meta1 = meta[4] | meta[5] << 8 | meta[6] << 16 | meta[7] << 24;
+            for (int k = 0; k < 3; ++k) {
+                N.q[k][0] = ql[k][0] | ql[k][1] << 8 | ql[k][2] << 16 | ql[k][3] << 24;
+                N.q[k][1] = ql[k][4] | ql[k][5] << 8 | ql[k][6] << 16 | ql[k][7] << 24;
+                N.q[k][2] = qh[k][0] | qh[k][1] << 8 | qh[k][2] << 16 | qh[k][3] << 24;
+                N.q[k][3] = qh[k][4] | qh[k][5] << 8 | qh[k][6] << 16 | qh[k][7] << 24;
+            }
+        }
+        triStart += scanT.back();
+        items.swap(next);
+    }
+}
+
 // ------------------------------------------------------------------ scene view
 struct SceneView {
     const optpt_scene *s;
@@ -363,8 +555,8 @@ float boxEntry(const Box &b, F3 o, F3 inv, float tmin, float tmax)
         tn = std::fmax(tn, std::fmin(a, c));
         tf = std::fmin(tf, std::fmax(a, c));
     }
-    tf *= 1.0000004f;
-    return tn <= std::fmin(tf, tmax) ? tn : INFINITY;
+    // widened by 2^-19 so equal-t candidates reach the index tie-break
+    return tn <= std::fmin(tf, tmax) * 1.0000019f ? tn : INFINITY;
 }
 float safeInv(float d) { return 1.0f / (std::fabs(d) > 1e-20f ? d : std::copysign(1e-20f, d)); }
 
@@ -844,6 +1036,25 @@ int orc_bvh(void *view, uint32_t *codes, int32_t *order, int32_t *nodes4, uint32
             return -1;
         memcpy(nodes4, B.nodes4.data(), B.nodes4.size() * 4);
     }
+    return 0;
+}
+
+// The compressed 8-wide BVH collapsed from this view's BVH2: 80-byte nodes and
+// the primitive of every triangle slot. counts[0] = nodes.
+int orc_bvh8(void *view, void *nodes, uint32_t capacity, int32_t *order8, uint32_t *counts)
+{
+    const SceneView &sv = *(SceneView *)view;
+    std::vector<Node8> out;
+    std::vector<int> ord;
+    buildHostBvh8(sv.bvh, out, ord);
+    counts[0] = (uint32_t)out.size();
+    if (nodes) {
+        if (capacity < out.size())
+            return -1;
+        memcpy(nodes, out.data(), out.size() * sizeof(Node8));
+    }
+    if (order8)
+        memcpy(order8, ord.data(), ord.size() * sizeof(int));
     return 0;
 }
 

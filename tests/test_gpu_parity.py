@@ -55,9 +55,9 @@ def test_bsdf_2pow24_queries_vs_fp64_oracle(cuda_dev):
     assert ok, bad
 
 
-def _scene_from(arrays_scene, leaf=4):
+def _scene_from(arrays_scene, leaf=4, width=8):
     import optix_pt_gb300 as opt
-    return opt.Renderer(arrays_scene, leaf_size=leaf)
+    return opt.Renderer(arrays_scene, leaf_size=leaf, bvh_width=width)
 
 
 def _scenes():
@@ -85,10 +85,27 @@ def test_morton_codes_leaf_order_and_topology(cuda_dev, leaf):
         r.close()
 
 
-def test_closest_hit_bit_exact(cuda_dev):
+@pytest.mark.parametrize("leaf", [1, 3, 4])
+def test_bvh8_collapse_matches_host(cuda_dev, leaf):
+    """The compressed 8-wide BVH, byte for byte: node records (quantised
+    boxes, slots, child and triangle bases) and the triangle order."""
+    for name, sc in _scenes():
+        r = _scene_from(sc, leaf, 8)
+        v = orc.SceneView(sc.struct, leaf)
+        hn, ho = v.bvh8(sc.num_triangles)
+        gn, go = r.bvh8_nodes()
+        assert gn.shape == hn.shape, (name, gn.shape, hn.shape)
+        assert np.array_equal(gn, hn), "%s: %d node records differ" % (name, int((gn != hn).any(1).sum()))
+        assert np.array_equal(go, ho), name
+        assert r.stats()["bvh8Nodes"] == len(hn)
+        r.close()
+
+
+@pytest.mark.parametrize("width", [8, 2])
+def test_closest_hit_bit_exact(cuda_dev, width):
     rng = np.random.default_rng(7)
     for name, sc in _scenes():
-        r = _scene_from(sc)
+        r = _scene_from(sc, 4 if width == 2 else 3, width)
         v = orc.SceneView(sc.struct, 4)
         a = sc.arrays()["positions"] if hasattr(sc, "arrays") else sc.P
         lo, hi = a.min(0), a.max(0)
@@ -103,10 +120,11 @@ def test_closest_hit_bit_exact(cuda_dev):
         r.close()
 
 
-def test_occlusion_bit_exact(cuda_dev):
+@pytest.mark.parametrize("width", [8, 2])
+def test_occlusion_bit_exact(cuda_dev, width):
     rng = np.random.default_rng(8)
     for name, sc in _scenes()[:3]:
-        r = _scene_from(sc)
+        r = _scene_from(sc, 3, width)
         v = orc.SceneView(sc.struct, 4)
         a = sc.arrays()["positions"] if hasattr(sc, "arrays") else sc.P
         lo, hi = a.min(0), a.max(0)
@@ -135,7 +153,12 @@ def test_alpha_mask_and_blend(cuda_dev):
     for any_hit in (False, True):
         g = trace_on_gpu(r, rays, cuda_dev, any_hit)
         c = v.trace(rays, any_hit)
-        assert np.array_equal(g.view(np.int32), c.view(np.int32))
+        if any_hit:
+            # an occlusion query returns the first accepted triangle it finds,
+            # which depends on the tree; only "occluded or not" is canonical
+            assert np.array_equal(g[:, 3].view(np.int32) >= 0, c[:, 3].view(np.int32) >= 0)
+        else:
+            assert np.array_equal(g.view(np.int32), c.view(np.int32))
         prims = g[:, 3].view(np.int32)
         assert not np.isin(prims[prims >= 0] % 3, [1]).any()   # masked material never hit
     r.close()

@@ -70,6 +70,40 @@ def test_lbvh_invariants(built, n, dup, leaf):
     assert seen == used
 
 
+@pytest.mark.parametrize("n,dup,leaf", [(1, False, 3), (3, False, 3), (37, False, 3), (1000, True, 4),
+                                        (5000, False, 1)])
+def test_bvh8_collapse_invariants(built, n, dup, leaf):
+    s, keep, tris = _tri_soup(n, 6, dup)
+    v = orc.SceneView(s, leaf)
+    nodes, order8 = v.bvh8(n)
+    assert np.array_equal(np.sort(order8), np.arange(n))
+    w = nodes.view(np.uint32).reshape(len(nodes), 20)
+    seen_tris = np.zeros(n, np.int32)
+    reached = np.zeros(len(nodes), np.int32)
+    reached[0] = 1
+    for i in range(len(nodes)):
+        imask = w[i, 3] >> 24
+        child_base, tri_base = w[i, 4], w[i, 5]
+        meta = np.concatenate([w[i, 6:8].view(np.uint8)])
+        q = w[i, 8:20].view(np.uint8).reshape(3, 16)
+        rank = 0
+        for s in range(8):
+            if meta[s] == 0:
+                continue
+            assert (q[:, s] <= q[:, 8 + s]).all()            # lo <= hi after quantisation
+            if (imask >> s) & 1:
+                c = child_base + rank
+                assert c > i and c < len(nodes)
+                reached[c] += 1
+                rank += 1
+            else:
+                cnt, off = meta[s] >> 5, meta[s] & 31
+                assert 1 <= cnt <= max(leaf, 1) or (i == 0 and n <= leaf)
+                seen_tris[tri_base + off: tri_base + off + cnt] += 1
+    assert (seen_tris == 1).all()
+    assert (reached == 1).all()
+
+
 def test_traversal_equals_brute_force(built):
     n = 1000
     s, keep, tris = _tri_soup(n, 9)
