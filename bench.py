@@ -4,9 +4,11 @@ One step = one pass of the wavefront path tracer over one frame: 1 sample per
 pixel of the material-sweep workload (8x8 icosphere grid, 327,684 triangles,
 1920x1080, max depth 12, point light + quad emitter), i.e. one call of the
 reference's per-frame launch. Ray count = extension rays + shadow rays
-actually traced.
+actually traced. --workload terrain measures the 9,996,610-triangle textured,
+alpha-masked terrain (1920x1080, max depth 16) the same way.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload sweep|terrain]
 
 --impl reference times the reference algorithm's CPU restatement (the oracle
 integrator, FP32, all host threads) on a bounded band of rows of the same
@@ -28,8 +30,15 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = {"workload": "material sweep: 8x8 icospheres (subdiv 4) + ground, 327,684 tris, point light + quad emitter",
-            "scene": "spheres", "width": 1920, "height": 1080, "max_depth": 12, "spp_per_step": 1}
+WORKLOADS = {
+    "sweep": {"workload": "material sweep: 8x8 icospheres (subdiv 4) + ground, 327,684 tris, point light + quad emitter",
+              "scene": "spheres", "width": 1920, "height": 1080, "max_depth": 12, "spp_per_step": 1},
+    "terrain": {"workload": "terrain: 2048x2048-quad fBm height field + 20,000 rocks (30% glass) + 4,000 alpha-masked "
+                            "textured foliage cards, normal-mapped ground, 9,996,610 tris, sun quad emitter",
+                "scene": "terrain", "width": 1920, "height": 1080, "max_depth": 16, "spp_per_step": 1},
+}
+CPU_SPP = {"sweep": 36, "terrain": 32}  # CPU-baseline sample: about 10-30 s of host work
+WORKLOAD = dict(WORKLOADS["sweep"])
 METRIC = "Mrays/s (extension + shadow rays traced), progressive path tracing, 1 spp per step"
 NODE_BYTES = {8: 80, 2: 64}  # compressed BVH8 node, BVH2 node
 TRI_BYTES = 48       # one leaf-ordered triangle record (3 x float4)
@@ -146,7 +155,8 @@ def run_reference(args, rank, world):
         tot_rays += rays
         tot_samples += samples
     value = tot_rays / tot_t / 1e6
-    sample = "one step = the full 1920x1080 frame at 1 spp, depth 12, FP32 oracle integrator"
+    sample = "one step = the full %dx%d frame at 1 spp, depth %d, FP32 oracle integrator" % (
+        WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["max_depth"])
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -270,7 +280,7 @@ def run_ours(args, rank, world, local_rank):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     kname = {"extend": "kExtend", "shadow": "kShadow", "shade": "kShade"}.get(dominant)
     if kname and os.path.exists(tp):
-        rec = json.load(open(tp)).get(kname)
+        rec = json.load(open(tp)).get(args.workload, {}).get(kname)
         if rec and rec.get("rays_per_launch"):
             rays_kernel = prof["extensionRays"] if dominant != "shadow" else prof["shadowRays"]
             per_launch_rays = rays_kernel / max(1, prof["launches"][dominant])
@@ -289,7 +299,7 @@ def run_ours(args, rank, world, local_rank):
         threads = os.cpu_count()
         dt, crays, csamples = cpu_render_band(scene, h, threads, spp=args.cpu_spp)
         cpu = {"value": crays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": "the full 1920x1080 frame at %d spp, FP32 oracle integrator, %.1f s" % (args.cpu_spp, dt)}
+               "sample": "the full %dx%d frame at %d spp, FP32 oracle integrator, %.1f s" % (w, h, args.cpu_spp, dt)}
 
     passes_launches = 3 + 4 * WORKLOAD["max_depth"]
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -314,13 +324,17 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-spp", type=int, default=36)
+    ap.add_argument("--workload", default="sweep", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-spp", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8])
     ap.add_argument("--leaf-size", type=int, default=0)
     ap.add_argument("--block-size", type=int, default=0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    WORKLOAD.clear()
+    WORKLOAD.update(WORKLOADS[args.workload])
+    args.cpu_spp = args.cpu_spp or CPU_SPP[args.workload]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

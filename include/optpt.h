@@ -105,8 +105,9 @@ int optpt_scene_from_config(const char *sceneListPath, optpt_scene *out);
 
 typedef struct optpt_options {
     uint32_t sppBatch;   /* samples traced side by side in one wavefront (0 = auto) */
-    uint32_t blockSize;  /* threads per block for the wavefront kernels (0 = auto)  */
-    uint32_t leafSize;   /* maximum triangles per BVH leaf, 1..8 (0 = auto)          */
+    uint32_t blockSize;  /* threads per block for the wavefront kernels (0 = 128)   */
+    uint32_t leafSize;   /* maximum triangles per BVH leaf: 1..4 for the 8-wide BVH
+                          * (0 = 1), 1..8 for the binary one (0 = 4)                */
     uint32_t useGraph;   /* capture the bounce loop in a CUDA graph (default 1)      */
     uint32_t bvhWidth;   /* 8: compressed 8-wide BVH (default), 2: the binary LBVH   */
 } optpt_options;
@@ -235,6 +236,17 @@ int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32
  * GPU (different streams, no ordering) race and must be avoided. */
 int optpt_relmse_noalloc(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
                          void *stream);
+
+/* ------------------------------------------------------------------ tensor-core self-test */
+
+/* Checks this library's tcgen05 operand descriptors and TMEM layouts (no
+ * counterpart in the reference, whose OptiX path has no tensor-core code).
+ * Device arrays, BF16 bits row-major: A[128][64], B[64][64], G[128][64],
+ * X[128][64]. Writes c[128][64] = A B^T (FP32) and dwRaw[128][64] = the TMEM
+ * lanes x columns holding G^T X (M = 64); *status = 1 if the MMA completion
+ * wait expired. One CTA; asynchronous on `stream`. */
+int optpt_tc_selftest(const uint16_t *A, const uint16_t *B, const uint16_t *G, const uint16_t *X, float *c,
+                      float *dwRaw, int *status, void *stream);
 
 /* ------------------------------------------------------------------ parity entry points */
 

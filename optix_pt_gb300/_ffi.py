@@ -163,6 +163,7 @@ _sigs = {
     "optpt_bvh_nodes": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
     "optpt_bvh8_nodes": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), _P]),
     "optpt_bsdf_batch": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P]),
+    "optpt_tc_selftest": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
 }
 EXPORTS = tuple(_sigs)
 for _name, (_res, _args) in _sigs.items():

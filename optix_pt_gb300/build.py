@@ -18,7 +18,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(ROOT, "_build", "optpt")
 LIB = os.path.join(OUT_DIR, "liboptpt.so")
 
-CUDA_SOURCES = ["bvh_build.cu", "bvh8_build.cu", "wavefront.cu", "engine.cu", "metrics.cu"]
+CUDA_SOURCES = ["bvh_build.cu", "bvh8_build.cu", "wavefront.cu", "engine.cu", "metrics.cu", "guide.cu"]
 CXX_SOURCES = ["scenes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

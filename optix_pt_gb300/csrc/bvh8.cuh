@@ -32,6 +32,12 @@ OPT_D uint32_t byteOf(uint4 v, int k)  // k in 0..15
     return (w >> ((k & 3) * 8)) & 0xFFu;
 }
 
+// Byte k (0..3) of w as a float, exactly: 0x4B0000qq is 2^23 + q.
+OPT_D float byteToFloat(uint32_t w, int k)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)k)) - 8388608.0f;
+}
+
 template <bool ANY, class AlphaFn, class Counter = NoCount>
 OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, float3 o, float3 d,
                      float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &&ctr = Counter())
@@ -56,21 +62,32 @@ OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restric
         const float sx = __uint_as_float((ew & 0xFFu) << 23), sy = __uint_as_float(((ew >> 8) & 0xFFu) << 23),
                     sz = __uint_as_float(((ew >> 16) & 0xFFu) << 23);
         const uint32_t imask = ew >> 24;
-        // t = (p + q * s - o) * inv = q * (s * inv) + (p - o) * inv
+        // t = (p + q * s - o) * inv = q * (s * inv) + (p - o) * inv. The ray's
+        // direction signs pick the near plane of each axis (lo for a positive
+        // direction) once per node.
         const float axs = sx * inv.x, ays = sy * inv.y, azs = sz * inv.z;
         const float bx = (a.x - o.x) * inv.x, by = (a.y - o.y) * inv.y, bz = (a.z - o.z) * inv.z;
+        const bool px = inv.x >= 0.0f, py = inv.y >= 0.0f, pz = inv.z >= 0.0f;
+        const uint32_t nx0 = px ? qx.x : qx.z, nx1 = px ? qx.y : qx.w, fx0 = px ? qx.z : qx.x, fx1 = px ? qx.w : qx.y;
+        const uint32_t ny0 = py ? qy.x : qy.z, ny1 = py ? qy.y : qy.w, fy0 = py ? qy.z : qy.x, fy1 = py ? qy.w : qy.y;
+        const uint32_t nz0 = pz ? qz.x : qz.z, nz1 = pz ? qz.y : qz.w, fz0 = pz ? qz.z : qz.x, fz1 = pz ? qz.w : qz.y;
+        const float tlim = tcur * BOX_WIDEN;
         uint32_t ihits = 0, lhits = 0;
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
             const uint32_t meta = byteOf(b, 8 + s);
             if (meta == 0u)
                 continue;
-            const float x0 = fmaf((float)byteOf(qx, s), axs, bx), x1 = fmaf((float)byteOf(qx, 8 + s), axs, bx);
-            const float y0 = fmaf((float)byteOf(qy, s), ays, by), y1 = fmaf((float)byteOf(qy, 8 + s), ays, by);
-            const float z0 = fmaf((float)byteOf(qz, s), azs, bz), z1 = fmaf((float)byteOf(qz, 8 + s), azs, bz);
-            const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
-            const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
-            if (tn <= fminf(tf, tcur) * BOX_WIDEN) {
+            const int k = s & 3;
+            const float xn = fmaf(byteToFloat(s < 4 ? nx0 : nx1, k), axs, bx);
+            const float xf = fmaf(byteToFloat(s < 4 ? fx0 : fx1, k), axs, bx);
+            const float yn = fmaf(byteToFloat(s < 4 ? ny0 : ny1, k), ays, by);
+            const float yf = fmaf(byteToFloat(s < 4 ? fy0 : fy1, k), ays, by);
+            const float zn = fmaf(byteToFloat(s < 4 ? nz0 : nz1, k), azs, bz);
+            const float zf = fmaf(byteToFloat(s < 4 ? fz0 : fz1, k), azs, bz);
+            const float tn = fmaxf(fmaxf(xn, yn), fmaxf(zn, tmin));
+            const float tf = fminf(fminf(xf, yf), zf) * BOX_WIDEN;
+            if (tn <= fminf(tf, tlim)) {
                 if ((imask >> s) & 1u)
                     ihits |= 1u << ((uint32_t)s ^ oct);
                 else

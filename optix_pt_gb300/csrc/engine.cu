@@ -46,8 +46,6 @@ template <class T> cudaError_t upload(T *&dst, const T *src, size_t count)
     return cudaMemcpy(dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
 }
 
-float3 f3(const float *p) { return make_float3(p[0], p[1], p[2]); }
-
 }  // namespace
 
 struct optpt_renderer {
@@ -249,7 +247,7 @@ int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
     r->lp.accumFrameBuffer = (float *)r->acc.accumFrameBuffer;
     r->hostFb.assign(npix * 4, 0.0f);
     r->hostFbValid = false;
-    const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 256;
+    const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 128;
     r->shape.block = blk;
     r->shape.gridGenerate = occupancyGrid(0, blk);
     const bool wide = r->bvh.nodes8 != nullptr;
@@ -446,7 +444,7 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         return fail(OPTPT_ERR_INVALID, "bvhWidth must be 2 or 8");
     }
     if (r->opt.leafSize == 0)
-        r->opt.leafSize = r->opt.bvhWidth == 8 ? 3 : 4;
+        r->opt.leafSize = r->opt.bvhWidth == 8 ? 1 : 4;
     // BVH8 leaves address up to 32 triangles per node with 5-bit offsets.
     const uint32_t maxLeaf = r->opt.bvhWidth == 8 ? 4u : 8u;
     if (r->opt.leafSize > maxLeaf)

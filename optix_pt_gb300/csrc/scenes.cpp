@@ -377,6 +377,320 @@ int buildSpheres(uint32_t seed, optpt_scene *out)
     return OPTPT_OK;
 }
 
+// ------------------------------------------------------------------ terrain
+// Lattice value noise with smooth interpolation and fractal sums, all in
+// double from integer hashes (identical on every host).
+double hashUnit(int64_t x, int64_t y, uint64_t seed)
+{
+    uint64_t h = (uint64_t)x * 0x9E3779B97F4A7C15ull ^ (uint64_t)y * 0xC2B2AE3D27D4EB4Full ^ seed * 0x165667B19E3779F9ull;
+    h ^= h >> 29;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 32;
+    return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+double valueNoise(double x, double y, uint64_t seed)
+{
+    const double fx = std::floor(x), fy = std::floor(y);
+    const int64_t ix = (int64_t)fx, iy = (int64_t)fy;
+    double tx = x - fx, ty = y - fy;
+    tx = tx * tx * (3.0 - 2.0 * tx);
+    ty = ty * ty * (3.0 - 2.0 * ty);
+    const double a = hashUnit(ix, iy, seed), b = hashUnit(ix + 1, iy, seed);
+    const double c = hashUnit(ix, iy + 1, seed), d = hashUnit(ix + 1, iy + 1, seed);
+    return (a + (b - a) * tx) + ((c + (d - c) * tx) - (a + (b - a) * tx)) * ty;
+}
+double fbm(double x, double y, uint64_t seed, int octaves)
+{
+    double s = 0.0, amp = 0.5, f = 1.0;
+    for (int o = 0; o < octaves; ++o) {
+        s += amp * valueNoise(x * f, y * f, seed + (uint64_t)o * 1013u);
+        amp *= 0.5;
+        f *= 2.0;
+    }
+    return s;  // in [0, 1)
+}
+
+// 1024^2 RGBA8 textures of the alpha-masked quads: colour noise with an fBm
+// alpha (about half below the 0.5 cutoff), and the tangent-space normal map
+// of an fBm height field. Both tile.
+void makeFoliageTextures(int res, uint64_t seed, std::vector<uint8_t> &albedo, std::vector<uint8_t> &normal)
+{
+    albedo.resize((size_t)res * res * 4);
+    normal.resize((size_t)res * res * 4);
+    const double period = 16.0;
+    auto tiled = [&](double u, double v, uint64_t sd) {
+        // bilinear blend of four offsets makes the pattern tile with the texture
+        const double a = fbm(u, v, sd, 5), b = fbm(u - period, v, sd, 5);
+        const double c = fbm(u, v - period, sd, 5), d = fbm(u - period, v - period, sd, 5);
+        const double wu = u / period, wv = v / period;
+        return (a * (1 - wu) + b * wu) * (1 - wv) + (c * (1 - wu) + d * wu) * wv;
+    };
+    std::vector<double> h((size_t)res * res);
+    for (int y = 0; y < res; ++y)
+        for (int x = 0; x < res; ++x) {
+            const double u = period * x / res, v = period * y / res;
+            const double n = tiled(u, v, seed), m = tiled(u * 2.0, v * 2.0, seed + 7);
+            uint8_t *p = &albedo[4 * ((size_t)y * res + x)];
+            p[0] = (uint8_t)std::lround(255.0 * (0.20 + 0.25 * m));
+            p[1] = (uint8_t)std::lround(255.0 * (0.35 + 0.45 * n));
+            p[2] = (uint8_t)std::lround(255.0 * (0.10 + 0.15 * m));
+            p[3] = (uint8_t)std::lround(255.0 * std::fmin(1.0, std::fmax(0.0, (n - 0.5) * 6.0 + 0.5)));
+            h[(size_t)y * res + x] = tiled(u * 3.0, v * 3.0, seed + 13);
+        }
+    for (int y = 0; y < res; ++y)
+        for (int x = 0; x < res; ++x) {
+            auto H = [&](int xx, int yy) { return h[(size_t)((yy + res) % res) * res + (size_t)((xx + res) % res)]; };
+            const double dx = (H(x + 1, y) - H(x - 1, y)) * 0.5 * res * 0.02, dy = (H(x, y + 1) - H(x, y - 1)) * 0.5 * res * 0.02;
+            Vec n = normv(Vec{-dx, -dy, 1.0});
+            uint8_t *p = &normal[4 * ((size_t)y * res + x)];
+            p[0] = (uint8_t)std::lround(255.0 * (n.x * 0.5 + 0.5));
+            p[1] = (uint8_t)std::lround(255.0 * (n.y * 0.5 + 0.5));
+            p[2] = (uint8_t)std::lround(255.0 * (n.z * 0.5 + 0.5));
+            p[3] = 255;
+        }
+}
+
+// Traversal-bound landscape: a grid x grid quad fBm terrain (seed 7), rocks
+// (flattened, randomly scaled and rotated subdivision-1 icospheres; 30% rough
+// glass: ior 1.5, transmission 1, roughness U(0, 0.3)), alpha-masked quads
+// (20% of the rock count) with an RGBA8 noise texture (cutoff 0.5) and a
+// tangent-space normal map, and a sun-like quad emitter. grid = 2048,
+// rocks = 20000, texture 1024^2 gives the 10-million-triangle workload.
+int buildTerrain(uint32_t seed, int grid, int rocks, int texRes, optpt_scene *out)
+{
+    Builder b;
+    b.withNormals = true;
+    SceneRng rng{0x7e44a100ull + seed};
+    const double extent = 200.0, amp = 18.0;
+    auto height = [&](double x, double z) { return amp * fbm(x / 25.0 + 100.0, z / 25.0 + 100.0, 7, 6); };
+
+    MaterialData ground = baseMaterial(0.35, 0.30, 0.22);
+    ground.roughness = 0.9f;
+    const int groundM = b.addMaterial(ground);
+    MaterialData sun = baseMaterial(0.0, 0.0, 0.0);
+    setv(sun.emission, 40.0, 37.0, 32.0);
+    const int sunM = b.addMaterial(sun);
+    std::vector<int> rockM, glassM;
+    for (int k = 0; k < 12; ++k) {
+        MaterialData m = baseMaterial(rng.range(0.25, 0.6), rng.range(0.22, 0.5), rng.range(0.2, 0.45));
+        m.roughness = (float)rng.range(0.4, 1.0);
+        m.metallic = k % 4 == 0 ? 1.0f : 0.0f;
+        m.specular = k % 3 == 0 ? 0.5f : 0.0f;
+        rockM.push_back(b.addMaterial(m));
+    }
+    for (int k = 0; k < 16; ++k) {
+        MaterialData m = baseMaterial(rng.range(0.8, 1.0), rng.range(0.85, 1.0), rng.range(0.85, 1.0));
+        m.transmissionWeight = 1.0f;
+        m.ior = 1.5f;
+        m.roughness = (float)rng.range(0.0, 0.3);
+        m.specular = 1.0f;
+        glassM.push_back(b.addMaterial(m));
+    }
+    MaterialData leaf = baseMaterial(1.0, 1.0, 1.0);
+    leaf.roughness = 0.7f;
+    leaf.alphaMode = AM_MASK;
+    leaf.alphaCutoff = 0.5f;
+    leaf.baseColourTexture = 0;
+    leaf.hasBaseColourTexture = 1;
+    leaf.normalTexture = 1;
+    leaf.hasNormalTexture = 1;
+    leaf.baseColourTexTf.scale[0] = leaf.baseColourTexTf.scale[1] = 2.0f;
+    leaf.normalTexTf.scale[0] = leaf.normalTexTf.scale[1] = 2.0f;
+    const int leafM = b.addMaterial(leaf);
+
+    // terrain: (grid + 1)^2 vertices with finite-difference normals
+    const int nv = grid + 1;
+    const double cell = extent / grid;
+    const int base = (int)(b.pos.size() / 3);
+    std::vector<double> hs((size_t)nv * nv);
+    for (int j = 0; j < nv; ++j)
+        for (int i = 0; i < nv; ++i)
+            hs[(size_t)j * nv + i] = height(-extent / 2 + i * cell, -extent / 2 + j * cell);
+    for (int j = 0; j < nv; ++j)
+        for (int i = 0; i < nv; ++i) {
+            auto H = [&](int ii, int jj) {
+                ii = std::min(std::max(ii, 0), nv - 1);
+                jj = std::min(std::max(jj, 0), nv - 1);
+                return hs[(size_t)jj * nv + ii];
+            };
+            Vec n = normv(Vec{-(H(i + 1, j) - H(i - 1, j)) / (2 * cell), 1.0, -(H(i, j + 1) - H(i, j - 1)) / (2 * cell)});
+            const int v = b.addVertex(Vec{-extent / 2 + i * cell, hs[(size_t)j * nv + i], -extent / 2 + j * cell}, n);
+            b.tc[2 * v] = (float)(i * 0.25);
+            b.tc[2 * v + 1] = (float)(j * 0.25);
+        }
+    for (int j = 0; j < grid; ++j)
+        for (int i = 0; i < grid; ++i) {
+            const int a = base + j * nv + i, c = a + 1, d = a + nv, e = d + 1;
+            b.tri(a, d, c, groundM);  // normals face +y: cross(d - a, c - a) has +y
+            b.tri(c, d, e, groundM);
+        }
+    // rocks
+    for (int k = 0; k < rocks; ++k) {
+        const double x = rng.range(-extent * 0.45, extent * 0.45), z = rng.range(-extent * 0.45, extent * 0.45);
+        const double s = rng.range(0.3, 1.5), flat = rng.range(0.3, 0.6), yaw = rng.range(0.0, 360.0);
+        const bool glass = rng.uniform() < 0.3;
+        const int m = glass ? glassM[(size_t)(rng.uniform() * glassM.size()) % glassM.size()]
+                            : rockM[(size_t)(rng.uniform() * rockM.size()) % rockM.size()];
+        b.icosphere(Vec{x, height(x, z) + s * flat * 0.6, z}, s, 1, m, Vec{1.0, flat, rng.range(0.6, 1.0)}, yaw);
+    }
+    // alpha-masked quads (vertical, textured)
+    const int quads = rocks / 5;
+    for (int k = 0; k < quads; ++k) {
+        const double x = rng.range(-extent * 0.45, extent * 0.45), z = rng.range(-extent * 0.45, extent * 0.45);
+        const double w = rng.range(1.0, 3.0), hgt = rng.range(1.0, 3.0), yaw = rng.range(0.0, 3.14159265358979);
+        const double y0 = height(x, z) - 0.1;
+        const Vec ax{std::cos(yaw) * w * 0.5, 0.0, std::sin(yaw) * w * 0.5};
+        const Vec c{x, y0, z};
+        const Vec n = normv(Vec{-std::sin(yaw), 0.0, std::cos(yaw)});
+        const Vec p[4] = {c - ax, c + ax, c + ax + Vec{0, hgt, 0}, c - ax + Vec{0, hgt, 0}};
+        const double uv[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+        int id[4];
+        for (int q = 0; q < 4; ++q) {
+            id[q] = b.addVertex(p[q], n);
+            b.tc[2 * id[q]] = (float)uv[q][0];
+            b.tc[2 * id[q] + 1] = (float)uv[q][1];
+        }
+        b.tri(id[0], id[1], id[2], leafM);
+        b.tri(id[0], id[2], id[3], leafM);
+    }
+    // sun: a 40 x 40 quad high above, facing down towards the terrain centre
+    b.quad({60, 250, -20}, {100, 250, -20}, {100, 250, 20}, {60, 250, 20}, {0, -1, 0}, sunM);
+    finish(b, out);
+    out->texCoords = dup(b.tc);
+    std::vector<uint8_t> alb, nrm;
+    makeFoliageTextures(texRes, seed, alb, nrm);
+    optpt_texture *tex = (optpt_texture *)calloc(2, sizeof(optpt_texture));
+    tex[0].width = tex[0].height = (uint32_t)texRes;
+    tex[0].rgba = dup(alb);
+    tex[0].srgb = 1;
+    tex[1].width = tex[1].height = (uint32_t)texRes;
+    tex[1].rgba = dup(nrm);
+    tex[1].srgb = 0;
+    out->textures = tex;
+    out->numTextures = 2;
+    const double ex = -70.0, ez = -75.0;
+    setv(out->camEye, ex, height(ex, ez) + 14.0, ez);
+    setv(out->camTarget, 10.0, height(10.0, 10.0), 10.0);
+    setv(out->camUp, 0.0, 1.0, 0.0);
+    out->camFovYDeg = 45.0f;
+    out->resX = 1920;
+    out->resY = 1080;
+    setv(out->bgColour, 0.30, 0.45, 0.70);
+    out->spp = 64;
+    out->maxDepth = 16;
+    return OPTPT_OK;
+}
+
+// Indirect-lit interior: a closed 10 x 4 x 6 room (x in [-5, 5], y in [0, 4],
+// z in [-3, 3]) whose only opening is a 1 x 2 doorway in the x = +5 wall; a
+// 3 x 3 quad emitter of radiance 50 stands outside, facing the doorway, and
+// the background is black, so everything inside is lit through the doorway.
+// Furniture: tables and chairs of boxes, shelves, and `balls` icospheres of
+// `subdiv` levels on the floor, table tops and shelves; materials are diffuse
+// (roughness 1, no specular lobe) or GGX metal (roughness U(0.1, 0.6)).
+int buildInterior(uint32_t seed, int balls, int subdiv, optpt_scene *out)
+{
+    Builder b;
+    b.withNormals = true;
+    SceneRng rng{0x1d00a7ull + seed};
+    MaterialData wall = baseMaterial(0.72, 0.70, 0.66);
+    wall.specular = 0.0f;
+    const int wallM = b.addMaterial(wall);
+    MaterialData floorMat = baseMaterial(0.45, 0.32, 0.20);
+    floorMat.specular = 0.0f;
+    const int floorM = b.addMaterial(floorMat);
+    MaterialData light = baseMaterial(0.0, 0.0, 0.0);
+    setv(light.emission, 50.0, 50.0, 50.0);
+    const int lightM = b.addMaterial(light);
+    std::vector<int> furnM;
+    for (int k = 0; k < 16; ++k) {
+        MaterialData m = baseMaterial(rng.range(0.2, 0.9), rng.range(0.2, 0.9), rng.range(0.2, 0.9));
+        if (k % 2 == 0) {
+            m.metallic = 1.0f;
+            m.roughness = (float)rng.range(0.1, 0.6);
+        } else {
+            m.specular = 0.0f;
+        }
+        furnM.push_back(b.addMaterial(m));
+    }
+    auto pick = [&]() { return furnM[(size_t)(rng.uniform() * furnM.size()) % furnM.size()]; };
+
+    const double X = 5.0, Y = 4.0, Z = 3.0, dz = 0.5, dy = 2.0;
+    b.quad({-X, 0, -Z}, {X, 0, -Z}, {X, 0, Z}, {-X, 0, Z}, {0, 1, 0}, floorM);      // floor
+    b.quad({-X, Y, -Z}, {X, Y, -Z}, {X, Y, Z}, {-X, Y, Z}, {0, -1, 0}, wallM);      // ceiling
+    b.quad({-X, 0, -Z}, {X, 0, -Z}, {X, Y, -Z}, {-X, Y, -Z}, {0, 0, 1}, wallM);     // back (z = -3)
+    b.quad({-X, 0, Z}, {X, 0, Z}, {X, Y, Z}, {-X, Y, Z}, {0, 0, -1}, wallM);        // front (z = +3)
+    b.quad({-X, 0, -Z}, {-X, 0, Z}, {-X, Y, Z}, {-X, Y, -Z}, {1, 0, 0}, wallM);     // x = -5
+    // x = +5 wall around the doorway z in [-0.5, 0.5], y in [0, 2]
+    b.quad({X, 0, -Z}, {X, 0, -dz}, {X, Y, -dz}, {X, Y, -Z}, {-1, 0, 0}, wallM);
+    b.quad({X, 0, dz}, {X, 0, Z}, {X, Y, Z}, {X, Y, dz}, {-1, 0, 0}, wallM);
+    b.quad({X, dy, -dz}, {X, dy, dz}, {X, Y, dz}, {X, Y, -dz}, {-1, 0, 0}, wallM);
+    // outside: the emitter, facing the doorway
+    b.quad({X + 2.5, 0.0, -1.5}, {X + 2.5, 0.0, 1.5}, {X + 2.5, 3.0, 1.5}, {X + 2.5, 3.0, -1.5}, {-1, 0, 0}, lightM);
+
+    // tables (top + 4 legs) with chairs, keeping a lane from the doorway clear
+    std::vector<Vec> tops;
+    for (int t = 0; t < 6; ++t) {
+        const double cx = -3.6 + 1.4 * t, cz = (t % 2 == 0) ? -1.7 : 1.7;
+        const int m = pick();
+        b.box({cx, 0.74, cz}, {0.5, 0.03, 0.4}, 0.0, m);
+        for (int l = 0; l < 4; ++l)
+            b.box({cx + (l & 1 ? 0.44 : -0.44), 0.36, cz + (l & 2 ? 0.34 : -0.34)}, {0.03, 0.36, 0.03}, 0.0, m);
+        tops.push_back({cx, 0.77, cz});
+        for (int c = 0; c < 2; ++c) {
+            const double ox = c == 0 ? -0.75 : 0.75;
+            const int cm = pick();
+            b.box({cx + ox, 0.45, cz}, {0.2, 0.03, 0.2}, 0.0, cm);
+            b.box({cx + ox + (c == 0 ? -0.18 : 0.18), 0.75, cz}, {0.02, 0.3, 0.2}, 0.0, cm);
+            for (int l = 0; l < 4; ++l)
+                b.box({cx + ox + (l & 1 ? 0.17 : -0.17), 0.21, cz + (l & 2 ? 0.17 : -0.17)}, {0.02, 0.21, 0.02}, 0.0, cm);
+        }
+    }
+    // shelves along the back and front walls
+    std::vector<Vec> shelves;
+    for (int s = 0; s < 4; ++s) {
+        const double cx = -3.0 + 2.0 * s, cz = (s % 2 == 0) ? -2.75 : 2.75;
+        const int m = pick();
+        for (int level = 0; level < 4; ++level) {
+            b.box({cx, 0.3 + 0.6 * level, cz}, {0.7, 0.02, 0.2}, 0.0, m);
+            shelves.push_back({cx, 0.32 + 0.6 * level, cz});
+        }
+        b.box({cx - 0.7, 1.1, cz}, {0.02, 1.1, 0.2}, 0.0, m);
+        b.box({cx + 0.7, 1.1, cz}, {0.02, 1.1, 0.2}, 0.0, m);
+    }
+    // icospheres: on table tops, shelves and the floor
+    for (int k = 0; k < balls; ++k) {
+        const double u = rng.uniform();
+        const int m = pick();
+        if (u < 0.3) {
+            const Vec &t = tops[(size_t)(rng.uniform() * tops.size()) % tops.size()];
+            const double r = rng.range(0.05, 0.12);
+            b.icosphere({t.x + rng.range(-0.38, 0.38), t.y + r, t.z + rng.range(-0.28, 0.28)}, r, subdiv, m);
+        } else if (u < 0.6) {
+            const Vec &s = shelves[(size_t)(rng.uniform() * shelves.size()) % shelves.size()];
+            const double r = rng.range(0.04, 0.1);
+            b.icosphere({s.x + rng.range(-0.6, 0.6), s.y + r, s.z + rng.range(-0.1, 0.1)}, r, subdiv, m);
+        } else {
+            const double r = rng.range(0.1, 0.35);
+            double x = rng.range(-X + 0.4, X - 0.6), z = rng.range(-Z + 0.4, Z - 0.4);
+            if (x > 2.5 && std::fabs(z) < 0.9)  // keep the doorway lane clear
+                z = z < 0 ? z - 0.9 : z + 0.9;
+            b.icosphere({x, r, z}, r, subdiv, m);
+        }
+    }
+    finish(b, out);
+    setv(out->camEye, -4.6, 1.6, -2.2);
+    setv(out->camTarget, 1.5, 0.9, 1.2);
+    setv(out->camUp, 0.0, 1.0, 0.0);
+    out->camFovYDeg = 60.0f;
+    out->resX = 1280;
+    out->resY = 720;
+    setv(out->bgColour, 0.0, 0.0, 0.0);
+    out->spp = 64;
+    out->maxDepth = 12;
+    return OPTPT_OK;
+}
+
 // ------------------------------------------------------------------ JSON
 // A small recursive-descent JSON reader for the scene-selection files (the
 // reference uses rapidjson, src/scene_desc.cpp:50-153).
@@ -577,6 +891,14 @@ int optpt_scene_procedural(const char *name, uint32_t seed, optpt_scene *out)
         return buildCornell(seed, out);
     if (strcmp(name, "spheres") == 0)
         return buildSpheres(seed, out);
+    if (strcmp(name, "terrain") == 0)
+        return buildTerrain(seed, 2048, 20000, 1024, out);
+    if (strcmp(name, "terrain_small") == 0)
+        return buildTerrain(seed, 96, 400, 128, out);
+    if (strcmp(name, "interior") == 0)
+        return buildInterior(seed, 380, 4, out);
+    if (strcmp(name, "interior_small") == 0)
+        return buildInterior(seed, 60, 2, out);
     return optpt_internal_set_error(OPTPT_ERR_INVALID, (std::string("unknown procedural scene '") + name + "'").c_str());
 }
 

@@ -1,0 +1,134 @@
+// Fifth-generation tensor-core (tcgen05) helpers for sm_103a, as inline PTX:
+// TMEM allocation, BF16 x BF16 -> FP32 MMA with shared-memory operand
+// descriptors, completion through an mbarrier, and TMEM -> register loads.
+//
+// Operand layout (no swizzle): matrices are tiled into "core matrices" of
+// 8 rows x 16 bytes (8 BF16), each stored as 128 contiguous bytes. For a
+// row-major tile X[r][c] (r = 0..R-1, c = 0..63) this library stores element
+// (r, c) at byte
+//     (r / 8) * 1024 + (c / 8) * 128 + (r % 8) * 16 + (c % 8) * 2
+// (tiles are 64 columns wide, so one 8-row group spans 1024 bytes). The same
+// bytes serve two operand views:
+//   * K-major with K = c (rows r = M or N): LBO = 128 (next 8 columns),
+//     SBO = 1024 (next 8 rows);
+//   * MN-major with K = r and M/N = c: LBO = 1024 (next 8 K-rows),
+//     SBO = 128 (next 8 M/N elements).
+// Every wait on an mbarrier is bounded; on expiry the caller gets false.
+#pragma once
+#include <cstdint>
+
+namespace tc {
+
+__device__ __forceinline__ uint32_t smemAddr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Byte offset of element (r, c) in a 64-column tile.
+__host__ __device__ __forceinline__ uint32_t tileOffset(uint32_t r, uint32_t c)
+{
+    return (r >> 3) * 1024u + (c >> 3) * 128u + (r & 7u) * 16u + (c & 7u) * 2u;
+}
+
+// Shared-memory matrix descriptor (SWIZZLE_NONE): start address, leading and
+// stride byte offsets (all >> 4), descriptor version 1 at bits 46-47.
+__device__ __forceinline__ uint64_t smemDesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: BF16 A and B, FP32 D; aMN / bMN select
+// MN-major operands (otherwise K-major); N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idescBf16(uint32_t M, uint32_t N, bool aMN, bool bMN)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((aMN ? 1u : 0u) << 15) | ((bMN ? 1u : 0u) << 16) |
+           ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+// --- TMEM allocation (one warp) ------------------------------------------
+__device__ __forceinline__ void tmemAlloc(uint32_t *dstSmem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(dstSmem)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmemFree(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// --- ordering -------------------------------------------------------------
+__device__ __forceinline__ void fenceBeforeSync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fenceAfterSync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// Generic-proxy shared-memory writes made visible to the tensor core.
+__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// --- mbarrier ---------------------------------------------------------------
+__device__ __forceinline__ void mbarInit(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbarTryWait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smemAddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase with the given parity to complete; false after
+// `limit` polls (each try_wait also suspends for a hardware time slice).
+__device__ __forceinline__ bool mbarWait(uint64_t *bar, uint32_t parity, uint32_t limit = 1u << 22)
+{
+    for (uint32_t i = 0; i < limit; ++i)
+        if (mbarTryWait(bar, parity))
+            return true;
+    return false;
+}
+
+// --- MMA --------------------------------------------------------------------
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
+__device__ __forceinline__ void mma(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc, bool accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dTmem),
+        "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate ? 1u : 0u)
+        : "memory");
+}
+// Arrives on `bar` once all previously issued MMAs of this thread complete.
+__device__ __forceinline__ void commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemAddr(bar))
+                 : "memory");
+}
+
+// --- TMEM -> registers ------------------------------------------------------
+// 32 lanes x 16 columns: thread i of the warp gets lane (taddr.lane + i),
+// columns taddr.col .. +15. The warp must address its own lane quarter. The
+// load completes (tcgen05.wait::ld) before the values are returned.
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+        v[k] = __uint_as_float(r[k]);
+}
+
+}  // namespace tc

@@ -49,13 +49,13 @@ OPT_D float4 sampleTexture(const uint32_t *__restrict__ texels, int4 info, float
     const int ws = info.w & 0xF, wt = (info.w >> 4) & 0xF;
     const bool srgb = (info.w >> 8) & 1, point = (info.w >> 9) & 1;
     const uint32_t *img = texels + info.x;
-    float x = u * (float)W, y = v * (float)H;
     if (point) {
+        const float x = __fmul_rn(u, (float)W), y = __fmul_rn(v, (float)H);
         int ix = wrapTexel((int)floorf(x), W, ws), iy = wrapTexel((int)floorf(y), H, wt);
         return texelToFloat(__ldg(img + iy * W + ix), srgb);
     }
-    x -= 0.5f;
-    y -= 0.5f;
+    // Every multiply-add is an explicit fmaf, in the order the host oracle uses.
+    const float x = fmaf(u, (float)W, -0.5f), y = fmaf(v, (float)H, -0.5f);
     float fx0 = floorf(x), fy0 = floorf(y);
     float ax = x - fx0, ay = y - fy0;
     int x0 = (int)fx0, y0 = (int)fy0;
@@ -63,10 +63,18 @@ OPT_D float4 sampleTexture(const uint32_t *__restrict__ texels, int4 info, float
     int ya = wrapTexel(y0, H, wt), yb = wrapTexel(y0 + 1, H, wt);
     float4 c00 = texelToFloat(__ldg(img + ya * W + xa), srgb), c10 = texelToFloat(__ldg(img + ya * W + xb), srgb);
     float4 c01 = texelToFloat(__ldg(img + yb * W + xa), srgb), c11 = texelToFloat(__ldg(img + yb * W + xb), srgb);
-    float4 r;
-    r.x = (c00.x + (c10.x - c00.x) * ax) + ((c01.x + (c11.x - c01.x) * ax) - (c00.x + (c10.x - c00.x) * ax)) * ay;
-    r.y = (c00.y + (c10.y - c00.y) * ax) + ((c01.y + (c11.y - c01.y) * ax) - (c00.y + (c10.y - c00.y) * ax)) * ay;
-    r.z = (c00.z + (c10.z - c00.z) * ax) + ((c01.z + (c11.z - c01.z) * ax) - (c00.z + (c10.z - c00.z) * ax)) * ay;
-    r.w = (c00.w + (c10.w - c00.w) * ax) + ((c01.w + (c11.w - c01.w) * ax) - (c00.w + (c10.w - c00.w) * ax)) * ay;
-    return r;
+    auto bl = [&](float a00, float a10, float a01, float a11) {
+        const float top = fmaf(a10 - a00, ax, a00), bot = fmaf(a11 - a01, ax, a01);
+        return fmaf(bot - top, ay, top);
+    };
+    return make_float4(bl(c00.x, c10.x, c01.x, c11.x), bl(c00.y, c10.y, c01.y, c11.y), bl(c00.z, c10.z, c01.z, c11.z),
+                       bl(c00.w, c10.w, c01.w, c11.w));
+}
+
+// Barycentric interpolation of a texture coordinate: w t0 + u t1 + v t2 with
+// w = 1 - u - v, as explicit fmaf (identical on the host).
+OPT_D float baryInterp(float u, float v, float t0, float t1, float t2)
+{
+    const float w = (1.0f - u) - v;
+    return fmaf(v, t2, fmaf(u, t1, __fmul_rn(w, t0)));
 }

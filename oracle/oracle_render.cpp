@@ -570,6 +570,13 @@ struct AlphaCtx {
     float shadowXi;  // < 0: radiance ray
 };
 float sampleTex(const SceneView &sv, int tex, float u, float v, float out[4]);
+// w t0 + u t1 + v t2 with w = 1 - u - v, as the same fused multiply-adds the
+// device uses, so texture lookups agree bit for bit.
+template <class R> R baryInterp(R u, R v, R t0, R t1, R t2)
+{
+    const R w = (R(1) - u) - v;
+    return std::fma(v, t2, std::fma(u, t1, w * t0));
+}
 bool alphaAccept(const AlphaCtx &a, int prim, float u, float v)
 {
     const optpt_scene *s = a.sv->s;
@@ -579,9 +586,8 @@ bool alphaAccept(const AlphaCtx &a, int prim, float u, float v)
     float alpha = M.baseColour[3];
     if (M.hasBaseColourTexture && M.baseColourTexture >= 0 && s->texCoords) {
         const int *I = s->triIndices + 3 * prim;
-        float w = 1.0f - u - v;
-        float tu = w * s->texCoords[2 * I[0]] + u * s->texCoords[2 * I[1]] + v * s->texCoords[2 * I[2]];
-        float tv = w * s->texCoords[2 * I[0] + 1] + u * s->texCoords[2 * I[1] + 1] + v * s->texCoords[2 * I[2] + 1];
+        float tu = baryInterp(u, v, s->texCoords[2 * I[0]], s->texCoords[2 * I[1]], s->texCoords[2 * I[2]]);
+        float tv = baryInterp(u, v, s->texCoords[2 * I[0] + 1], s->texCoords[2 * I[1] + 1], s->texCoords[2 * I[2] + 1]);
         float c[4];
         sampleTex(*a.sv, M.baseColourTexture, tu, tv, c);
         alpha *= c[3];
@@ -687,9 +693,7 @@ float sampleTex(const SceneView &sv, int tex, float u, float v, float out[4])
 {
     const optpt_texture &t = sv.s->textures[tex];
     const int W = (int)t.width, H = (int)t.height;
-    float x = u * (float)W, y = v * (float)H;
-    x -= 0.5f;
-    y -= 0.5f;
+    const float x = std::fma(u, (float)W, -0.5f), y = std::fma(v, (float)H, -0.5f);
     float fx0 = std::floor(x), fy0 = std::floor(y);
     float ax = x - fx0, ay = y - fy0;
     int x0 = (int)fx0, y0 = (int)fy0;
@@ -698,8 +702,8 @@ float sampleTex(const SceneView &sv, int tex, float u, float v, float out[4])
     for (int c = 0; c < 4; ++c) {
         float c00 = texChan(sv, t, xa, ya, c), c10 = texChan(sv, t, xb, ya, c);
         float c01 = texChan(sv, t, xa, yb, c), c11 = texChan(sv, t, xb, yb, c);
-        float top = c00 + (c10 - c00) * ax, bot = c01 + (c11 - c01) * ax;
-        out[c] = top + (bot - top) * ay;
+        const float top = std::fma(c10 - c00, ax, c00), bot = std::fma(c11 - c01, ax, c01);
+        out[c] = std::fma(bot - top, ay, top);
     }
     return out[3];
 }
@@ -768,14 +772,13 @@ V3<R> tracePath(const SceneView &sv, const RenderParams &rp, uint32_t pixel, uin
         const bool anyTex = M.hasBaseColourTexture || M.hasNormalTexture || M.hasMetallicRoughnessTexture ||
                             M.hasEmissiveTexture || M.hasSheenColourTexture || M.hasSheenRoughnessTexture;
         if (anyTex && s->texCoords) {
-            const R w = R(1) - u - v;
-            tcu = w * R(s->texCoords[2 * I[0]]) + u * R(s->texCoords[2 * I[1]]) + v * R(s->texCoords[2 * I[2]]);
-            tcv = w * R(s->texCoords[2 * I[0] + 1]) + u * R(s->texCoords[2 * I[1] + 1]) +
-                  v * R(s->texCoords[2 * I[2] + 1]);
+            tcu = baryInterp<R>(u, v, R(s->texCoords[2 * I[0]]), R(s->texCoords[2 * I[1]]), R(s->texCoords[2 * I[2]]));
+            tcv = baryInterp<R>(u, v, R(s->texCoords[2 * I[0] + 1]), R(s->texCoords[2 * I[1] + 1]),
+                                R(s->texCoords[2 * I[2] + 1]));
         }
         auto tex = [&](int id, const TextureTransform &tf, float out[4]) {
-            float tu = (float)(tcu * R(tf.scale[0]) + R(tf.offset[0]));
-            float tv = (float)(tcv * R(tf.scale[1]) + R(tf.offset[1]));
+            float tu = (float)std::fma(tcu, R(tf.scale[0]), R(tf.offset[0]));
+            float tv = (float)std::fma(tcv, R(tf.scale[1]), R(tf.offset[1]));
             sampleTex(sv, id, tu, tv, out);
         };
         V3<R> normal = interpN;
@@ -939,13 +942,13 @@ V3<R> tracePath(const SceneView &sv, const RenderParams &rp, uint32_t pixel, uin
                     nv = area2(P.x, P.y, q2.x, q2.y, q0.x, q0.y);
                     ood = R(1) / mm.z;
                 }
-                const R bu = nu * ood, bv = nv * ood, bw = R(1) - bu - bv;
+                const R bu = nu * ood, bv = nv * ood;
                 const float *c0 = s->texCoords + 2 * EI[0], *c1 = s->texCoords + 2 * EI[1], *c2 = s->texCoords + 2 * EI[2];
-                const R etu = bw * R(c0[0]) + bu * R(c1[0]) + bv * R(c2[0]);
-                const R etv = bw * R(c0[1]) + bu * R(c1[1]) + bv * R(c2[1]);
+                const R etu = baryInterp<R>(bu, bv, R(c0[0]), R(c1[0]), R(c2[0]));
+                const R etv = baryInterp<R>(bu, bv, R(c0[1]), R(c1[1]), R(c2[1]));
                 float c[4];
-                sampleTex(sv, EM.emissiveTexture, (float)(etu * R(M.emissiveTexTf.scale[0]) + R(M.emissiveTexTf.offset[0])),
-                          (float)(etv * R(M.emissiveTexTf.scale[1]) + R(M.emissiveTexTf.offset[1])), c);
+                sampleTex(sv, EM.emissiveTexture, (float)std::fma(etu, R(M.emissiveTexTf.scale[0]), R(M.emissiveTexTf.offset[0])),
+                          (float)std::fma(etv, R(M.emissiveTexTf.scale[1]), R(M.emissiveTexTf.offset[1])), c);
                 Le = Le * v3<R>(R(c[0]), R(c[1]), R(c[2]));
             }
             const R cosX = std::fmax(R(0), dot(normal, ldir));

@@ -109,3 +109,42 @@ def soup(n, seed, dup=False, scale=0.15):
     P = (c[:, None, :] + rng.normal(scale=scale, size=(n, 3, 3))).reshape(-1, 3).astype(np.float32)
     I = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
     return P, I
+
+
+def render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None, **renderer_kw):
+    """GPU render (sample indices from 0) and an oracle render of the same
+    frame (sample indices from cpu_base): ((sum, sumsq, n) GPU, (sum, sumsq,
+    n) oracle, GPU stats, oracle ray counts)."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    from oracle import oracle as orc
+    r = opt.Renderer(scene, spp_batch=batch or 0, **renderer_kw)
+    r.setupOutputBuffer(w, h)
+    r.render(spp_gpu, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    s, q, n = r.accum()
+    lp = r.launch_params()
+    cam = list(lp.eye) + list(lp.U) + list(lp.V) + list(lp.W) + list(lp.bgColour)
+    v = orc.SceneView(scene.struct, 4)
+    cs, cq, cnt = v.render(cam, w, h, lp.seed, cpu_base, spp_cpu, lp.maxDepth, precision=precision)
+    st = r.stats()
+    r.close()
+    return (s.reshape(-1, 3), q.reshape(-1, 3), n), (cs, cq, spp_cpu), st, cnt
+
+
+def pixel_stats(g, c):
+    """Per-pixel z scores of two independent Monte Carlo estimates: (fraction
+    of live pixels with z > 3, |frame mean difference|, its standard error,
+    GPU means, oracle means, live mask)."""
+    (gs, gq, gn), (cs, cq, cn) = g, c
+    gm, cm = gs / gn, cs / cn
+    gv = np.maximum(gq / gn - gm ** 2, 0) / gn
+    cv = np.maximum(cq / cn - cm ** 2, 0) / cn
+    var = gv + cv
+    live = var > 0
+    z = np.zeros_like(gm)
+    z[live] = np.abs(gm - cm)[live] / np.sqrt(var[live])
+    frac = float((z[live] > 3.0).mean()) if live.any() else 0.0
+    se = np.sqrt(var.sum()) / var.size
+    return frac, abs(gm.mean() - cm.mean()), se, gm, cm, live

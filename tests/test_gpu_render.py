@@ -9,7 +9,7 @@
 import numpy as np
 import pytest
 
-from gpu_util import ArrayScene, material
+from gpu_util import ArrayScene, material, pixel_stats, render_pair
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
@@ -20,36 +20,8 @@ def _camera(r):
     return list(lp.eye) + list(lp.U) + list(lp.V) + list(lp.W) + list(lp.bgColour), lp
 
 
-def _render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None):
-    import torch
-
-    import optix_pt_gb300 as opt
-    r = opt.Renderer(scene, spp_batch=batch or 0)
-    r.setupOutputBuffer(w, h)
-    r.render(spp_gpu, torch.cuda.current_stream())
-    torch.cuda.synchronize()
-    s, q, n = r.accum()
-    cam, lp = _camera(r)
-    v = orc.SceneView(scene.struct, 4)
-    cs, cq, cnt = v.render(cam, w, h, lp.seed, cpu_base, spp_cpu, lp.maxDepth, precision=precision)
-    st = r.stats()
-    r.close()
-    return (s.reshape(-1, 3), q.reshape(-1, 3), n), (cs, cq, spp_cpu), st, cnt
-
-
-def _stats(g, c):
-    (gs, gq, gn), (cs, cq, cn) = g, c
-    gm, cm = gs / gn, cs / cn
-    gv = np.maximum(gq / gn - gm ** 2, 0) / gn
-    cv = np.maximum(cq / cn - cm ** 2, 0) / cn
-    var = gv + cv
-    live = var > 0
-    z = np.zeros_like(gm)
-    z[live] = np.abs(gm - cm)[live] / np.sqrt(var[live])
-    frac = float((z[live] > 3.0).mean()) if live.any() else 0.0
-    # frame mean and its standard error
-    se = np.sqrt(var.sum()) / var.size
-    return frac, abs(gm.mean() - cm.mean()), se, gm, cm, live
+_render_pair = render_pair
+_stats = pixel_stats
 
 
 @pytest.mark.parametrize("name,w,h,spp", [("cornell", 96, 96, 1), ("cornell", 96, 96, 4), ("spheres", 160, 90, 2)])
