@@ -237,6 +237,46 @@ int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32
 int optpt_relmse_noalloc(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
                          void *stream);
 
+/* ------------------------------------------------------------------ learned guiding network */
+
+/* The path-guiding network (no counterpart in the reference, which samples
+ * by the BSDF only): a 16-level hash-grid encoding of position plus the
+ * shading normal and outgoing direction, 4 hidden layers of 64 (BF16 on the
+ * tensor cores, FP32 accumulation), and 8 von Mises-Fisher lobes out. Created
+ * over a world-space box [lo, hi]; parameters initialised from `seed`. */
+typedef struct optpt_guide optpt_guide;
+int optpt_guide_create(const float lo[3], const float hi[3], uint32_t seed, optpt_guide **out);
+int optpt_guide_destroy(optpt_guide *g);
+
+/* Host copies of the FP32 parameters: mlp = 5 x 64 x 64 (W[layer][out][in]),
+ * hash = 16 x 2^19 x 2. write = 1 uploads them (and refreshes the BF16 and
+ * FP16 working copies), 0 downloads. Either pointer may be NULL. */
+int optpt_guide_params(optpt_guide *g, float *mlp, float *hash, int write);
+
+/* The level resolutions, dense-indexing flags and the world -> unit-cube map
+ * (u = (p - lo) * invExt), host arrays of 16, 16, 3, 3. */
+int optpt_guide_levels(optpt_guide *g, float *res, uint32_t *dense, float *lo, float *invExt);
+
+/* Mixtures for n shading points. Device arrays: queries = 3 float4 each
+ * (position, normal, outgoing direction; w ignored); mixtures = 80 bytes
+ * each: per lobe (mu.xyz, kappa) as 4 halves, then the 8 weights as halves. */
+int optpt_guide_infer(optpt_guide *g, const float *queries, uint32_t n, void *mixtures, void *stream);
+
+/* Gradient of the batch loss sum_i -c_i log q(wi_i), c_i = weight_i / sum of
+ * weights. Device arrays: samples = 4 float4 each ((position, weight),
+ * normal, outgoing, incoming direction wi); *count (device) = samples used,
+ * at most `capacity`. Host outputs (NULL to skip): dMlp (5 x 64 x 64), dHash
+ * (16 x 2^19 x 2), loss. Synchronises `stream`. */
+int optpt_guide_gradients(optpt_guide *g, const float *samples, const uint32_t *count, uint32_t capacity,
+                          float *dMlp, float *dHash, double *loss, void *stream);
+
+/* One Adam step (lr 1e-2) on the batch's gradient; asynchronous. */
+int optpt_guide_train_step(optpt_guide *g, const float *samples, const uint32_t *count, uint32_t capacity,
+                           void *stream);
+
+/* *status = 1 if a tensor-core completion wait expired; the last batch loss. */
+int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss);
+
 /* ------------------------------------------------------------------ tensor-core self-test */
 
 /* Checks this library's tcgen05 operand descriptors and TMEM layouts (no

@@ -305,3 +305,64 @@ def relmse(sum_ptr, n_samples, ref_ptr, num_pixels, out_ptr, stream=None):
 def bsdf_batch(queries_ptr, results_ptr, n, stream=None):
     """Device BSDF queries (optpt_bsdf_query -> optpt_bsdf_result), device pointers."""
     check(lib.optpt_bsdf_batch(queries_ptr, results_ptr, n, _stream_handle(stream)))
+
+
+class Guide:
+    """The learned path-guiding network (hash grid + MLP on the tensor cores,
+    8 vMF lobes out) over the world-space box [lo, hi]."""
+
+    MLP_PARAMS = 5 * 64 * 64
+    HASH_PARAMS = 16 * (1 << 19) * 2
+
+    def __init__(self, lo, hi, seed=1):
+        h = ctypes.c_void_p()
+        check(lib.optpt_guide_create(_ffi.f3(*lo), _ffi.f3(*hi), seed, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.optpt_guide_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def params(self):
+        mlp = np.zeros(self.MLP_PARAMS, np.float32)
+        hsh = np.zeros(self.HASH_PARAMS, np.float32)
+        check(lib.optpt_guide_params(self._h, mlp.ctypes.data, hsh.ctypes.data, 0))
+        return mlp, hsh
+
+    def set_params(self, mlp=None, hash_params=None):
+        m = None if mlp is None else np.ascontiguousarray(mlp, np.float32)
+        hp = None if hash_params is None else np.ascontiguousarray(hash_params, np.float32)
+        check(lib.optpt_guide_params(self._h, None if m is None else m.ctypes.data,
+                                     None if hp is None else hp.ctypes.data, 1))
+
+    def geometry(self):
+        """(level resolutions, dense flags, lo, invExt) as the oracle takes them."""
+        res = np.zeros(16, np.float32)
+        dense = np.zeros(16, np.uint32)
+        lo = np.zeros(3, np.float32)
+        inv = np.zeros(3, np.float32)
+        check(lib.optpt_guide_levels(self._h, res.ctypes.data, dense.ctypes.data, lo.ctypes.data, inv.ctypes.data))
+        return res, dense, lo, inv
+
+    def infer(self, queries_ptr, n, mixtures_ptr, stream=None):
+        check(lib.optpt_guide_infer(self._h, queries_ptr, n, mixtures_ptr, _stream_handle(stream)))
+
+    def gradients(self, samples_ptr, count_ptr, capacity, stream=None):
+        dm = np.zeros(self.MLP_PARAMS, np.float32)
+        dh = np.zeros(self.HASH_PARAMS, np.float32)
+        loss = ctypes.c_double()
+        check(lib.optpt_guide_gradients(self._h, samples_ptr, count_ptr, capacity, dm.ctypes.data, dh.ctypes.data,
+                                        ctypes.byref(loss), _stream_handle(stream)))
+        return loss.value, dm, dh
+
+    def train_step(self, samples_ptr, count_ptr, capacity, stream=None):
+        check(lib.optpt_guide_train_step(self._h, samples_ptr, count_ptr, capacity, _stream_handle(stream)))
+
+    def status(self):
+        st = ctypes.c_int()
+        loss = ctypes.c_double()
+        check(lib.optpt_guide_status(self._h, ctypes.byref(st), ctypes.byref(loss)))
+        return st.value, loss.value

@@ -164,6 +164,15 @@ _sigs = {
     "optpt_bvh8_nodes": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), _P]),
     "optpt_bsdf_batch": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P]),
     "optpt_tc_selftest": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "optpt_guide_create": (ctypes.c_int, [f3, f3, ctypes.c_uint32, ctypes.POINTER(_P)]),
+    "optpt_guide_destroy": (ctypes.c_int, [_P]),
+    "optpt_guide_params": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
+    "optpt_guide_levels": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "optpt_guide_infer": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P, _P]),
+    "optpt_guide_gradients": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P, _P, ctypes.POINTER(ctypes.c_double),
+                                             _P]),
+    "optpt_guide_train_step": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P]),
+    "optpt_guide_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
 }
 EXPORTS = tuple(_sigs)
 for _name, (_res, _args) in _sigs.items():

@@ -1,0 +1,178 @@
+// Learned path guiding, device side shared by the network kernels and the
+// shading kernel: the multiresolution hash-grid position encoding (after
+// Mueller et al., "Instant Neural Graphics Primitives", SIGGRAPH 2022), the
+// network's input/output layout, and the von Mises-Fisher mixture the network
+// emits (evaluation, sampling and decoding; mixture parameterisation after
+// Dong et al., "Neural Parametric Mixtures for Path Guiding", SIGGRAPH 2023).
+#pragma once
+#include <cuda_fp16.h>
+#include <cstdint>
+#include "common.cuh"
+
+namespace guide {
+
+constexpr int LEVELS = 16;            // hash-grid levels
+constexpr int FEATS = 2;              // features per level
+constexpr uint32_t TABLE = 1u << 19;  // entries per level
+constexpr float RES_MIN = 16.0f, RES_MAX = 1024.0f;
+constexpr int WIDTH = 64;             // network width (inputs padded to 64)
+constexpr int LAYERS = 5;             // 64x64 weight matrices: in -> h1 -> h2 -> h3 -> h4 -> out
+constexpr int LOBES = 8;              // vMF lobes; outputs 5k..5k+4 = (mu raw xyz, log kappa, weight logit)
+constexpr int IN_NORMAL = 2 * LEVELS, IN_WO = IN_NORMAL + 3, IN_ONE = IN_WO + 3;
+constexpr float LOG_KAPPA_MIN = -3.0f, LOG_KAPPA_MAX = 8.0f;
+constexpr size_t HASH_PARAMS = (size_t)LEVELS * TABLE * FEATS;
+constexpr int MLP_PARAMS = LAYERS * WIDTH * WIDTH;
+
+// Grid resolution of level l: floor(RES_MIN * b^l), b = (RES_MAX/RES_MIN)^(1/(LEVELS-1)).
+// The host computes the table once (levelRes) so device and oracle agree.
+struct Levels {
+    float res[LEVELS];
+    uint32_t dense[LEVELS];  // 1: (res+1)^3 <= TABLE, direct indexing
+};
+
+OPT_HD uint32_t cornerIndex(uint32_t x, uint32_t y, uint32_t z, uint32_t res1, bool dense)
+{
+    if (dense)
+        return x + res1 * (y + res1 * z);
+    return (x * 1u ^ y * 2654435761u ^ z * 805459861u) & (TABLE - 1u);
+}
+
+// Trilinear corner c (bit 0 = x, 1 = y, 2 = z) of level `l` for a position
+// in the unit cube: the table entry and the weight.
+OPT_HD void corner(const Levels &L, int l, float px, float py, float pz, int c, uint32_t &entry, float &w)
+{
+    const float r = L.res[l];
+    const float gx = px * r, gy = py * r, gz = pz * r;
+    const float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    const float tx = gx - fx, ty = gy - fy, tz = gz - fz;
+    const uint32_t x = (uint32_t)fx + (c & 1), y = (uint32_t)fy + ((c >> 1) & 1), z = (uint32_t)fz + ((c >> 2) & 1);
+    w = ((c & 1) ? tx : 1.0f - tx) * (((c >> 1) & 1) ? ty : 1.0f - ty) * (((c >> 2) & 1) ? tz : 1.0f - tz);
+    entry = cornerIndex(x, y, z, (uint32_t)r + 1u, L.dense[l] != 0);
+}
+
+// ------------------------------------------------------------------ vMF mixture
+struct Lobe {
+    float3 mu;
+    float kappa, weight;
+};
+struct Mixture {
+    Lobe lobe[LOBES];
+};
+
+// Normalisation kappa / (2 pi (1 - exp(-2 kappa))), the isotropic 1/(4 pi) as kappa -> 0.
+OPT_D float vmfNorm(float kappa)
+{
+    if (kappa < 1e-4f)
+        return 0.25f * OPT_INV_PI;
+    return kappa * (0.5f * OPT_INV_PI) / -expm1f(-2.0f * kappa);
+}
+OPT_D float vmfPdf(const Lobe &L, float3 w)
+{
+    return vmfNorm(L.kappa) * expf(L.kappa * (dot3(L.mu, w) - 1.0f));
+}
+OPT_D float mixturePdf(const Mixture &m, float3 w)
+{
+    float p = 0.0f;
+#pragma unroll
+    for (int k = 0; k < LOBES; ++k)
+        p += m.lobe[k].weight * vmfPdf(m.lobe[k], w);
+    return p;
+}
+// Lobe by xi0 over the weights; direction by Jakob's stable inversion
+// ("Numerically stable sampling of the von Mises-Fisher distribution on S^2").
+OPT_D float3 mixtureSample(const Mixture &m, float xi0, float xi1, float xi2)
+{
+    int k = LOBES - 1;
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < LOBES; ++j) {
+        acc += m.lobe[j].weight;
+        if (xi0 < acc) {
+            k = j;
+            break;
+        }
+    }
+    const Lobe &L = m.lobe[k];
+    float w;
+    if (L.kappa < 1e-4f)
+        w = 1.0f - 2.0f * xi1;
+    else
+        w = 1.0f + logf(xi1 + (1.0f - xi1) * expf(-2.0f * L.kappa)) / L.kappa;
+    w = fminf(fmaxf(w, -1.0f), 1.0f);
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - w * w));
+    float sp, cp;
+    sincosf(2.0f * OPT_PI * xi2, &sp, &cp);
+    // frame around mu (Duff et al. 2017 branchless ONB)
+    const float3 n = L.mu;
+    const float sign = copysignf(1.0f, n.z);
+    const float a = -1.0f / (sign + n.z), b = n.x * n.y * a;
+    const float3 t = mk3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    const float3 bt = mk3(b, sign + n.y * n.y * a, -n.y);
+    return normalize3(w * n + (s * cp) * t + (s * sp) * bt);
+}
+
+// Network outputs o[0..39] -> mixture (softmax weights, exp kappa, unit mu).
+OPT_D void decodeOutputs(const float *o, Mixture &m)
+{
+    float mx = -1e30f;
+#pragma unroll
+    for (int k = 0; k < LOBES; ++k)
+        mx = fmaxf(mx, o[5 * k + 4]);
+    float sum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < LOBES; ++k) {
+        const float e = expf(o[5 * k + 4] - mx);
+        m.lobe[k].weight = e;
+        sum += e;
+        const float3 r = mk3(o[5 * k], o[5 * k + 1], o[5 * k + 2]);
+        const float len = sqrtf(dot3(r, r));
+        m.lobe[k].mu = len > 1e-12f ? r * (1.0f / len) : mk3(0.0f, 0.0f, 1.0f);
+        m.lobe[k].kappa = expf(fminf(fmaxf(o[5 * k + 3], LOG_KAPPA_MIN), LOG_KAPPA_MAX));
+    }
+    const float inv = 1.0f / sum;
+#pragma unroll
+    for (int k = 0; k < LOBES; ++k)
+        m.lobe[k].weight *= inv;
+}
+
+// Packed mixture as stored per ray between the inference and shading kernels:
+// per lobe (mu.xyz, kappa) as 4 halves, then the 8 weights as halves: 80 B.
+struct alignas(16) Packed {
+    uint4 q[5];
+};
+OPT_D void pack(const Mixture &m, Packed &p)
+{
+    __half h[40];
+#pragma unroll
+    for (int k = 0; k < LOBES; ++k) {
+        h[4 * k] = __float2half_rn(m.lobe[k].mu.x);
+        h[4 * k + 1] = __float2half_rn(m.lobe[k].mu.y);
+        h[4 * k + 2] = __float2half_rn(m.lobe[k].mu.z);
+        h[4 * k + 3] = __float2half_rn(fminf(m.lobe[k].kappa, 60000.0f));
+        h[32 + k] = __float2half_rn(m.lobe[k].weight);
+    }
+    memcpy(&p, h, sizeof(p));
+}
+// Decoded values are what sampling and evaluation both use, so the density
+// the shading kernel evaluates is exactly the one it samples from.
+OPT_D void unpack(const Packed &p, Mixture &m)
+{
+    __half h[40];
+    memcpy(h, &p, sizeof(p));
+    float sum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < LOBES; ++k) {
+        const float3 mu = mk3(__half2float(h[4 * k]), __half2float(h[4 * k + 1]), __half2float(h[4 * k + 2]));
+        const float len = sqrtf(dot3(mu, mu));
+        m.lobe[k].mu = len > 1e-6f ? mu * (1.0f / len) : mk3(0.0f, 0.0f, 1.0f);
+        m.lobe[k].kappa = __half2float(h[4 * k + 3]);
+        m.lobe[k].weight = __half2float(h[32 + k]);
+        sum += m.lobe[k].weight;
+    }
+    const float inv = sum > 0.0f ? 1.0f / sum : 0.0f;
+#pragma unroll
+    for (int k = 0; k < LOBES; ++k)
+        m.lobe[k].weight = sum > 0.0f ? m.lobe[k].weight * inv : 1.0f / LOBES;
+}
+
+}  // namespace guide

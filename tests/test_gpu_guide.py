@@ -3,6 +3,10 @@
 * tcgen05 operand layouts: a 128x64x64 K-major MMA and a 64x64x128 MN-major
   MMA (the weight-gradient shape) against FP32 products of the same BF16
   values.
+* The network's inference (mixture densities) and its gradients (loss,
+  weight and hash-table gradients) against the CPU oracle, which rounds to
+  BF16 where the kernels do; tolerances are relative.
+* Online training on a synthetic directional target.
 """
 import numpy as np
 import pytest
@@ -45,3 +49,151 @@ def test_tcgen05_operand_layouts(cuda_dev):
     assert lanes == {r: (r // 16) * 32 + r % 16 for r in range(64)}, lanes
     for r in range(64):
         np.testing.assert_allclose(dw[(r // 16) * 32 + r % 16], ref_dw[r], rtol=1e-5, atol=1e-4)
+
+
+# ------------------------------------------------------------------ network vs oracle
+LO, HI = (-5.0, 0.0, -3.0), (5.0, 4.0, 3.0)
+
+
+def _unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def _queries(rng, n):
+    q = np.zeros((n, 12), np.float32)
+    q[:, 0:3] = rng.uniform(LO, HI, (n, 3))
+    q[:, 4:7] = _unit(rng, n)
+    q[:, 8:11] = _unit(rng, n)
+    return q
+
+
+def _samples(rng, n):
+    s = np.zeros((n, 16), np.float32)
+    s[:, 0:3] = rng.uniform(LO, HI, (n, 3))
+    s[:, 3] = rng.exponential(1.0, n)
+    s[:, 4:7] = _unit(rng, n)
+    s[:, 8:11] = _unit(rng, n)
+    s[:, 12:15] = _unit(rng, n)
+    s[::17, 3] = 0.0          # zero-weight samples contribute nothing
+    s[5, 3] = np.nan          # non-finite weights are ignored
+    return s
+
+
+def _guide_with_features(seed):
+    import optix_pt_gb300 as opt
+    g = opt.Guide(LO, HI, seed=seed)
+    mlp, hsh = g.params()
+    rng = np.random.default_rng(seed)
+    hsh = rng.uniform(-0.5, 0.5, hsh.shape).astype(np.float32)   # features large enough to matter
+    g.set_params(hash_params=hsh)
+    return g, mlp, hsh
+
+
+def test_guide_inference_matches_oracle(cuda_dev):
+    import torch
+
+    from oracle import guide_oracle as go
+    g, mlp, hsh = _guide_with_features(11)
+    rng = np.random.default_rng(12)
+    n = 1000                                            # 7 full tiles + a ragged one
+    q = _queries(rng, n)
+    qd = torch.from_numpy(q).to(cuda_dev)
+    out = torch.zeros((n, 40), dtype=torch.float16, device=cuda_dev)
+    g.infer(qd.data_ptr(), n, out.data_ptr(), torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    assert g.status()[0] == 0
+    w, mu, kap = go.unpack(out.cpu().numpy())
+    o = go.infer(mlp, hsh, g.geometry(), q)
+    wr, mur, kapr, *_ = go.decode(o)
+    dirs = _unit(rng, n)
+    p_gpu = (w * go.vmf_pdf(mu, kap, dirs)[0]).sum(1)
+    p_ref = (wr * go.vmf_pdf(mur, kapr, dirs)[0]).sum(1)
+    rel = np.abs(p_gpu - p_ref) / p_ref
+    print("mixture pdf rel err: median %.2e p99 %.2e max %.2e" % (np.median(rel), np.quantile(rel, 0.99), rel.max()))
+    assert np.median(rel) < 1e-3 and np.quantile(rel, 0.99) < 5e-3
+    assert np.abs(w - wr).max() < 1e-2
+    g.close()
+
+
+def test_guide_gradients_match_oracle(cuda_dev):
+    import torch
+
+    from oracle import guide_oracle as go
+    g, mlp, hsh = _guide_with_features(21)
+    rng = np.random.default_rng(22)
+    n = 1000
+    s = _samples(rng, n)
+    sd = torch.from_numpy(s).to(cuda_dev)
+    cnt = torch.tensor([n], dtype=torch.int32, device=cuda_dev)
+    loss, dm, dh = g.gradients(sd.data_ptr(), cnt.data_ptr(), n, torch.cuda.current_stream())
+    rloss, rdm, rdh = go.gradients(mlp, hsh, g.geometry(), s)
+    print("loss gpu %.6f oracle %.6f" % (loss, rloss))
+    assert abs(loss - rloss) <= 1e-3 * abs(rloss)
+    dm = dm.reshape(5, 64, 64)
+    for l in range(5):
+        err = np.linalg.norm(dm[l] - rdm[l]) / np.linalg.norm(rdm[l])
+        print("layer %d dW rel err %.2e" % (l, err))
+        assert err < 5e-3, (l, err)
+    touched = rdh != 0
+    err = np.linalg.norm(dh[touched] - rdh[touched]) / np.linalg.norm(rdh[touched])
+    print("hash grad rel err %.2e over %d entries; untouched max %.1e" % (err, touched.sum(), np.abs(dh[~touched]).max()))
+    assert err < 5e-3
+    assert np.abs(dh[~touched]).max() == 0.0
+    g.close()
+
+
+def test_guide_training_learns_a_directional_target(cuda_dev):
+    """Online training on samples whose weight is a position-dependent lobe
+    (towards a fixed point): the learned mixture's density along the target
+    direction rises far above the untrained network's."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    from oracle import guide_oracle as go
+    g = opt.Guide(LO, HI, seed=5)
+    rng = np.random.default_rng(6)
+    target = np.array([4.0, 3.5, 0.0])
+
+    def batch(n):
+        s = np.zeros((n, 16), np.float32)
+        pos = rng.uniform(LO, HI, (n, 3))
+        d = target - pos
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        wi = _unit(rng, n)
+        kappa = 20.0
+        lobe = kappa / (2 * np.pi * (1 - np.exp(-2 * kappa))) * np.exp(kappa * ((wi * d).sum(1) - 1))
+        s[:, 0:3] = pos
+        s[:, 3] = lobe * 4 * np.pi            # target / uniform sampling pdf
+        s[:, 4:7] = _unit(rng, n)
+        s[:, 8:11] = _unit(rng, n)
+        s[:, 12:15] = wi
+        return s
+
+    def score():
+        n = 4096
+        q = np.zeros((n, 12), np.float32)
+        q[:, 0:3] = rng.uniform(LO, HI, (n, 3))
+        q[:, 4:7] = _unit(rng, n)
+        q[:, 8:11] = _unit(rng, n)
+        d = target - q[:, 0:3]
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        out = torch.zeros((n, 40), dtype=torch.float16, device=cuda_dev)
+        g.infer(torch.from_numpy(q).to(cuda_dev).data_ptr(), n, out.data_ptr(), torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        w, mu, kap = go.unpack(out.cpu().numpy())
+        return float(np.mean(np.log((w * go.vmf_pdf(mu, kap, d)[0]).sum(1))))
+
+    before = score()
+    n = 1 << 14
+    cnt = torch.tensor([n], dtype=torch.int32, device=cuda_dev)
+    for _ in range(300):
+        sd = torch.from_numpy(batch(n)).to(cuda_dev)
+        g.train_step(sd.data_ptr(), cnt.data_ptr(), n, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    assert g.status()[0] == 0
+    after = score()
+    print("mean log q(target direction): before %.3f after %.3f (uniform %.3f)" % (before, after, np.log(1 / (4 * np.pi))))
+    assert after > before + 2.0
+    assert after > np.log(20 / (2 * np.pi)) - 1.5   # near the target lobe's own peak density (log 1.16)
+    g.close()
