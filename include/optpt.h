@@ -187,10 +187,11 @@ int optpt_get_stats(optpt_renderer *r, optpt_stats *out);
 /* Per-kernel device time (ms) of one extra render of `spp` samples, launched
  * without a graph with CUDA events around each kernel on `stream`. Index:
  * 0 generate, 1 extend (closest hit), 2 shade, 3 shadow (occlusion),
- * 4 accumulate + tone map. Also returns the rays each kernel class traced. */
+ * 4 accumulate + tone map, 5 guiding inference, 6 guiding training (sample
+ * gather, gradients, Adam). Also returns the rays each kernel class traced. */
 typedef struct optpt_kernel_times {
-    double ms[5];
-    uint64_t launches[5];
+    double ms[7];
+    uint64_t launches[7];
     uint64_t extensionRays;
     uint64_t shadowRays;
 } optpt_kernel_times;
@@ -262,8 +263,8 @@ int optpt_guide_levels(optpt_guide *g, float *res, uint32_t *dense, float *lo, f
  * each: per lobe (mu.xyz, kappa) as 4 halves, then the 8 weights as halves. */
 int optpt_guide_infer(optpt_guide *g, const float *queries, uint32_t n, void *mixtures, void *stream);
 
-/* Gradient of the batch loss sum_i -c_i log q(wi_i), c_i = weight_i / sum of
- * weights. Device arrays: samples = 4 float4 each ((position, weight),
+/* Gradient of the batch loss sum_i -c_i log q(wi_i), c_i = min(weight_i, 16 *
+ * mean positive weight) / sum of weights. Device arrays: samples = 4 float4 each ((position, weight),
  * normal, outgoing, incoming direction wi); *count (device) = samples used,
  * at most `capacity`. Host outputs (NULL to skip): dMlp (5 x 64 x 64), dHash
  * (16 x 2^19 x 2), loss. Synchronises `stream`. */
@@ -274,8 +275,46 @@ int optpt_guide_gradients(optpt_guide *g, const float *samples, const uint32_t *
 int optpt_guide_train_step(optpt_guide *g, const float *samples, const uint32_t *count, uint32_t capacity,
                            void *stream);
 
-/* *status = 1 if a tensor-core completion wait expired; the last batch loss. */
-int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss);
+/* *status = 1 if a tensor-core completion wait expired; the loss and the
+ * number of samples of the last training step (either may be NULL). */
+int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss, double *lastSamples);
+
+/* Guided sampling in the renderer (replaces nothing in the reference, whose
+ * closest-hit program samples the BSDF only, cu/path_tracer.cu:522-581).
+ * mode 0: plain BSDF sampling (bit-identical to a renderer that never had
+ * guiding); 1: at guidable vertices (non-specular metal, diffuse, rough
+ * reflection and coat lobes) the direction comes from the network's mixture
+ * with probability 1/2, else from the BSDF, weighted by the one-sample MIS
+ * density, and the network trains online after every pass on the pass's own
+ * radiance estimates; 2: guided sampling with the network frozen. The
+ * network is created on first use over the scene's bounding box. */
+int optpt_set_guiding(optpt_renderer *r, int mode);
+/* Guiding controls (0 / 0.0 fields keep the current value):
+ * trainSteps   Adam steps per pass, each on one slice of the pass's samples (4)
+ * trainStride  one path in trainStride records training samples (1)
+ * maxDepth     vertices up to this depth are guided (all)
+ * alphaMax     probability of sampling the network's mixture (0.5) ...
+ * alphaRamp    ... reached after this many training steps, linearly (64)
+ * learningRate Adam step size (1e-2) */
+typedef struct optpt_guiding_options {
+    uint32_t trainSteps;
+    uint32_t trainStride;
+    uint32_t maxDepth;
+    float alphaMax;
+    float alphaRamp;
+    float learningRate;
+} optpt_guiding_options;
+int optpt_set_guiding_options(optpt_renderer *r, const optpt_guiding_options *o);
+int optpt_get_guiding_options(const optpt_renderer *r, optpt_guiding_options *o);
+
+/* The training samples gathered by the last pass (host copy of up to
+ * `capacity`, 16 floats each: (position, weight), (normal, -), (outgoing,
+ * -), (incoming wi, -)); *count = samples gathered. */
+int optpt_guiding_batch(optpt_renderer *r, float *samples, uint32_t capacity, uint32_t *count);
+
+/* The renderer's guiding network (NULL before guiding was first enabled),
+ * owned by the renderer. */
+int optpt_get_guide(optpt_renderer *r, optpt_guide **out);
 
 /* ------------------------------------------------------------------ tensor-core self-test */
 

@@ -260,7 +260,7 @@ class Renderer:
     def profile(self, spp, stream=None):
         kt = _ffi.KernelTimes()
         check(lib.optpt_render_profiled(self._h, spp, _stream_handle(stream), ctypes.byref(kt)))
-        names = ["generate", "extend", "shade", "shadow", "accumulate"]
+        names = ["generate", "extend", "shade", "shadow", "accumulate", "guide_infer", "guide_train"]
         return {"ms": dict(zip(names, list(kt.ms))), "launches": dict(zip(names, list(kt.launches))),
                 "extensionRays": kt.extensionRays, "shadowRays": kt.shadowRays}
 
@@ -288,6 +288,36 @@ class Renderer:
         order = np.zeros(max(self.scene.num_triangles, 1), np.int32)
         check(lib.optpt_bvh8_nodes(self._h, nodes.ctypes.data, cnt.value, ctypes.byref(cnt), order.ctypes.data))
         return nodes[:cnt.value], order[:self.scene.num_triangles]
+
+    def set_guiding(self, mode):
+        """0: plain BSDF sampling; 1: learned guiding with online training;
+        2: learned guiding, network frozen."""
+        check(lib.optpt_set_guiding(self._h, int(mode)))
+
+    def guiding_options(self, **kw):
+        """Reads, and with keyword arguments updates, the guiding controls
+        (trainSteps, trainStride, maxDepth, alphaMax, alphaRamp, learningRate)."""
+        o = _ffi.GuidingOptions()
+        if kw:
+            for k, v in kw.items():
+                setattr(o, k, v)
+            check(lib.optpt_set_guiding_options(self._h, ctypes.byref(o)))
+        check(lib.optpt_get_guiding_options(self._h, ctypes.byref(o)))
+        return {k: getattr(o, k) for k, _ in o._fields_}
+
+    def guiding_batch(self):
+        """The last pass's training samples, (n, 16) float32."""
+        n = ctypes.c_uint32()
+        check(lib.optpt_guiding_batch(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros((max(n.value, 1), 16), np.float32)
+        check(lib.optpt_guiding_batch(self._h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out[:n.value]
+
+    def guide(self):
+        """The renderer's guiding network (owned by the renderer), or None."""
+        h = ctypes.c_void_p()
+        check(lib.optpt_get_guide(self._h, ctypes.byref(h)))
+        return None if not h.value else Guide._borrow(h, self)
 
     def bvh_nodes(self):
         cnt = ctypes.c_uint32()
@@ -319,10 +349,17 @@ class Guide:
         check(lib.optpt_guide_create(_ffi.f3(*lo), _ffi.f3(*hi), seed, ctypes.byref(h)))
         self._h = h
 
+    @classmethod
+    def _borrow(cls, handle, owner):
+        g = cls.__new__(cls)
+        g._h = handle
+        g._owner = owner     # keeps the renderer (which frees the network) alive
+        return g
+
     def close(self):
-        if getattr(self, "_h", None):
+        if getattr(self, "_h", None) and getattr(self, "_owner", None) is None:
             lib.optpt_guide_destroy(self._h)
-            self._h = None
+        self._h = None
 
     __del__ = close
 
@@ -362,7 +399,9 @@ class Guide:
         check(lib.optpt_guide_train_step(self._h, samples_ptr, count_ptr, capacity, _stream_handle(stream)))
 
     def status(self):
+        """(tensor-core wait expired?, loss of the last step, its samples)."""
         st = ctypes.c_int()
         loss = ctypes.c_double()
-        check(lib.optpt_guide_status(self._h, ctypes.byref(st), ctypes.byref(loss)))
-        return st.value, loss.value
+        n = ctypes.c_double()
+        check(lib.optpt_guide_status(self._h, ctypes.byref(st), ctypes.byref(loss), ctypes.byref(n)))
+        return st.value, loss.value, n.value

@@ -107,8 +107,13 @@ class Stats(ctypes.Structure):
 
 
 class KernelTimes(ctypes.Structure):
-    _fields_ = [("ms", ctypes.c_double * 5), ("launches", ctypes.c_uint64 * 5), ("extensionRays", ctypes.c_uint64),
+    _fields_ = [("ms", ctypes.c_double * 7), ("launches", ctypes.c_uint64 * 7), ("extensionRays", ctypes.c_uint64),
                 ("shadowRays", ctypes.c_uint64)]
+
+
+class GuidingOptions(ctypes.Structure):
+    _fields_ = [("trainSteps", ctypes.c_uint32), ("trainStride", ctypes.c_uint32), ("maxDepth", ctypes.c_uint32),
+                ("alphaMax", ctypes.c_float), ("alphaRamp", ctypes.c_float), ("learningRate", ctypes.c_float)]
 
 
 class TraversalCounts(ctypes.Structure):
@@ -172,7 +177,13 @@ _sigs = {
     "optpt_guide_gradients": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P, _P, ctypes.POINTER(ctypes.c_double),
                                              _P]),
     "optpt_guide_train_step": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P]),
-    "optpt_guide_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    "optpt_guide_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
+    "optpt_set_guiding": (ctypes.c_int, [_H, ctypes.c_int]),
+    "optpt_get_guide": (ctypes.c_int, [_H, ctypes.POINTER(_P)]),
+    "optpt_guiding_batch": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
+    "optpt_set_guiding_options": (ctypes.c_int, [_H, ctypes.POINTER(GuidingOptions)]),
+    "optpt_get_guiding_options": (ctypes.c_int, [_H, ctypes.POINTER(GuidingOptions)]),
 }
 EXPORTS = tuple(_sigs)
 for _name, (_res, _args) in _sigs.items():

@@ -353,6 +353,49 @@ template <class U> OPT_D bool sampleBrdf(const MatMR &m, float3 wo, float3 xi, U
     return true;
 }
 
+// Lobes a learned proposal may be mixed with (one-sample MIS): those whose
+// sampler above has a closed-form density over all directions and whose
+// value does not depend on extra random draws. Excluded: specular (delta),
+// transmission (pdf without the refraction Jacobian, stochastic value) and
+// sheen (pdf 1).
+OPT_D bool guidable(uint32_t c)
+{
+    if (c & MF_SPECULAR)
+        return false;
+    if (c & MF_METAL)
+        return true;
+    if (c & MF_DIELECTRIC)
+        return !(c & MF_TRANSMISSION);
+    return (c & MF_COAT) != 0;
+}
+OPT_D bool reflectionLobe(uint32_t c) { return !(c & MF_METAL) && ((c & MF_REFLECTION) || !(c & MF_DIELECTRIC)); }
+// Density of sampleBrdf's direction for a guidable lobe, evaluated at l,
+// including the directions its sampler rejects (density 0 there, as a
+// rejected sample is a killed path).
+OPT_D float lobePdf(const MatMR &m, float3 l, float3 v)
+{
+    const uint32_t c = m.category;
+    if (c & MF_METAL)
+        return reflectionPdf(m, l, v);
+    if (reflectionLobe(c)) {
+        const float3 h = normalize3(l + v);
+        return (dot3(l, h) > 0.0f && dot3(l, m.n) > 0.0f) ? reflectionPdf(m, l, v) : 0.0f;
+    }
+    return dot3(m.n, l) * OPT_INV_PI;  // cosine-weighted diffuse
+}
+// Value sampleBrdf reports for direction l of a guidable lobe.
+OPT_D float3 lobeValue(const MatMR &m, float3 l, float3 v)
+{
+    const uint32_t c = m.category;
+    if (c & MF_METAL)
+        return metalBrdf(m, l, v);
+    if (reflectionLobe(c)) {
+        const float3 h = normalize3(l + v);
+        return (dot3(l, h) > 0.0f && dot3(l, m.n) > 0.0f) ? reflectionBrdf(m, l, v) : mk3s(0.0f);
+    }
+    return diffuseBrdf(m, l, v);
+}
+
 // The MaterialData fields that categorisation reads.
 struct CatIn {
     uint32_t category;

@@ -10,6 +10,7 @@
 #include <vector>
 #include "../../include/optpt.h"
 #include "engine.h"
+#include "guide_net.h"
 
 int uploadSrgbTable();
 
@@ -83,6 +84,18 @@ struct optpt_renderer {
 
     FrameConst *dFrameConst = nullptr;
 
+    // learned guiding (mode 0 off, 1 guided + online training, 2 guided, frozen)
+    optpt_guide *guide = nullptr;
+    int guideMode = 0;
+    void *gMix = nullptr;        // 80 B per path slot
+    float4 *gRec = nullptr;      // GUIDE_REC float4 per (training path, depth)
+    void *gBatch = nullptr;      // GuideSample per slot
+    uint32_t *gBatchCount = nullptr;
+    size_t gMixPaths = 0, gRecSlots = 0;
+    uint32_t gTrainStride = 1, gBatchCap = 1u << 18, gTrainSteps = 4, gMaxDepth = 0xFFFFFFFFu;
+    float gAlphaMax = 0.5f, gAlphaRamp = 64.0f, gLr = 1e-2f;
+    float sceneLo[3] = {0, 0, 0}, sceneHi[3] = {0, 0, 0};
+
     FrameParams frameParams() const
     {
         FrameParams fp{};
@@ -94,7 +107,34 @@ struct optpt_renderer {
         fp.maxDepth = lp.maxDepth;
         fp.state = dState;
         fp.fc = dFrameConst;
+        if (guideMode != 0) {
+            fp.guide.mix = gMix;
+            fp.guide.rec = gRec;
+            fp.guide.batch = gBatch;
+            fp.guide.batchCount = gBatchCount;
+            fp.guide.on = 1;
+            fp.guide.train = guideMode == 1 ? 1u : 0u;
+            fp.guide.trainStride = gTrainStride;
+            fp.guide.batchCapacity = gBatchCap;
+            fp.guide.step = guide->dStep;
+            fp.guide.alphaMax = gAlphaMax;
+            fp.guide.alphaRamp = gAlphaRamp;
+            fp.guide.maxDepth = gMaxDepth;
+        }
         return fp;
+    }
+
+    void freeGuideBuffers()
+    {
+        cudaFree(gMix);
+        cudaFree(gRec);
+        cudaFree(gBatch);
+        cudaFree(gBatchCount);
+        gMix = nullptr;
+        gRec = nullptr;
+        gBatch = nullptr;
+        gBatchCount = nullptr;
+        gMixPaths = gRecSlots = 0;
     }
 
     FrameConst frameConst() const
@@ -148,6 +188,11 @@ struct optpt_renderer {
     ~optpt_renderer()
     {
         freeFrame();
+        freeGuideBuffers();
+        if (guide) {
+            guideFree(guide);
+            delete guide;
+        }
         cudaFree(q.totals);
         cudaFree(q.counters);
         cudaFree(dState);
@@ -239,7 +284,7 @@ int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
     CUDA_OR_RETURN(cudaMemset(r->acc.sumSq, 0, sizeof(Acc4) * npix), "clear accum");
     CUDA_OR_RETURN(cudaMemset(r->acc.frameBuffer, 0, sizeof(float4) * npix), "clear fb");
     CUDA_OR_RETURN(cudaMemset(r->acc.accumFrameBuffer, 0, sizeof(float4) * npix), "clear fb");
-    CUDA_OR_RETURN(cudaMemset(r->dState, 0, sizeof(uint32_t) * 4), "clear state");
+    CUDA_OR_RETURN(cudaMemset(r->dState, 0, sizeof(uint32_t)), "clear state");
     r->lp.sample = 0;
     r->lp.w = width;
     r->lp.h = height;
@@ -260,8 +305,9 @@ int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
 }
 
 // One pass: sppBatch samples for every pixel.
-void enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaEvent_t *ev, int *kind,
-                 bool count = false)
+// Returns the number of events recorded (profiling), each tagged in `kind`.
+int enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaEvent_t *ev, int *kind,
+                bool count = false)
 {
     int e = 0;
     auto mark = [&](int k) {
@@ -272,21 +318,67 @@ void enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cuda
         }
     };
     cudaMemsetAsync(r->q.counters, 0, sizeof(uint32_t) * CNT_TOTAL, st);
+    if (fp.guide.train)
+        cudaMemsetAsync(fp.guide.batchCount, 0, sizeof(uint32_t), st);
     mark(0);
     launchGenerate(r->shape, fp, r->q, st);
     for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
         mark(1);
         launchExtend(r->shape, r->scene, fp, r->q, (int)d, st, count);
+        if (fp.guide.on && d < fp.maxDepth && d <= fp.guide.maxDepth) {
+            mark(5);
+            launchGuideInfer(r->guide, r->scene, fp, r->q, (int)d, st);
+        }
         mark(2);
         launchShade(r->shape, r->scene, fp, r->q, (int)d, st);
         mark(3);
         launchShadow(r->shape, r->scene, fp, r->q, (int)d, 0, st, count);
         launchShadow(r->shape, r->scene, fp, r->q, (int)d, 1, st, count);
     }
+    if (fp.guide.train) {
+        // online training on this pass's samples (before the pass count advances)
+        mark(6);
+        launchGuideGather(fp, r->q, st);
+        for (uint32_t k = 0; k < r->gTrainSteps; ++k) {  // minibatches of the pass's samples
+            guideGradients(r->guide, reinterpret_cast<const GuideSample *>(fp.guide.batch), fp.guide.batchCount,
+                           fp.guide.batchCapacity, st, k, r->gTrainSteps);
+            guideAdam(r->guide, st);
+        }
+    }
     mark(4);
     launchAccumulate(r->shape, fp, r->q, r->acc, st);
     launchAdvance(fp, r->dState, st);
-    mark(5);
+    mark(7);
+    return e;
+}
+
+// Guiding buffers sized for the current frame (paths per pass, max depth).
+int ensureGuideBuffers(optpt_renderer *r)
+{
+    if (r->guideMode == 0)
+        return OPTPT_OK;
+    const size_t paths = (size_t)r->w * r->h * r->sppBatch;
+    const size_t slots = ((paths + r->gTrainStride - 1) / r->gTrainStride) * std::max(1u, r->lp.maxDepth);
+    if (r->gMix && r->gMixPaths >= paths && r->gRecSlots >= slots)
+        return OPTPT_OK;
+    r->freeGuideBuffers();
+    cudaError_t e = cudaMalloc(&r->gMix, std::max<size_t>(paths, 1) * sizeof(guide::Packed));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&r->gRec, std::max<size_t>(slots, 1) * GUIDE_REC * sizeof(float4));
+    if (e == cudaSuccess)
+        e = cudaMemset(r->gRec, 0, std::max<size_t>(slots, 1) * GUIDE_REC * sizeof(float4));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&r->gBatch, (size_t)r->gBatchCap * sizeof(GuideSample));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&r->gBatchCount, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        r->freeGuideBuffers();
+        return fail(OPTPT_ERR_NOMEM, std::string("guiding buffers: ") + cudaGetErrorString(e));
+    }
+    r->gMixPaths = paths;
+    r->gRecSlots = slots;
+    r->graphDirty = true;
+    return OPTPT_OK;
 }
 
 int ensureGraph(optpt_renderer *r, cudaStream_t st)
@@ -462,6 +554,15 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         }
         const uint32_t nt = s->numTriangles;
         r->numTris = (int)nt;
+        for (int a = 0; a < 3; ++a) {
+            r->sceneLo[a] = nt ? 3.4e38f : 0.0f;
+            r->sceneHi[a] = nt ? -3.4e38f : 0.0f;
+        }
+        for (uint32_t v = 0; v < (nt ? s->numVertices : 0u); ++v)
+            for (int a = 0; a < 3; ++a) {
+                r->sceneLo[a] = std::min(r->sceneLo[a], s->positions[3 * v + a]);
+                r->sceneHi[a] = std::max(r->sceneHi[a], s->positions[3 * v + a]);
+            }
         std::vector<uint32_t> triFlags(nt);
         for (uint32_t t = 0; t < nt; ++t)
             triFlags[t] = s->materials[s->matIndices[t]].alphaMode != AM_OPAQUE ? TRI_FLAG_ALPHA : 0u;
@@ -552,6 +653,7 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
             (e = cudaMalloc((void **)&r->q.totals, sizeof(unsigned long long) * 8)) ||
             (e = cudaMemset(r->q.totals, 0, sizeof(unsigned long long) * 8)) ||
             (e = cudaMalloc((void **)&r->dState, sizeof(uint32_t) * 4)) ||
+            (e = cudaMemset(r->dState, 0, sizeof(uint32_t) * 4)) ||
             (e = cudaMalloc((void **)&r->dFrameConst, sizeof(FrameConst)))) {
             rc = cudaFail(e, "counters");
             break;
@@ -584,6 +686,96 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         return rc;
     }
     *out = r;
+    return OPTPT_OK;
+}
+
+int optpt_set_guiding(optpt_renderer *r, int mode)
+{
+    if (!r)
+        return fail(OPTPT_ERR_INVALID, "NULL renderer");
+    if (mode < 0 || mode > 2)
+        return fail(OPTPT_ERR_INVALID, "guiding mode must be 0 (off), 1 (guided, training) or 2 (guided, frozen)");
+    if (mode != 0 && !r->guide) {
+        optpt_guide *g = new optpt_guide();
+        int rc = guideCreate(g, r->sceneLo, r->sceneHi, r->lp.seed);
+        if (rc != OPTPT_OK) {
+            delete g;
+            return rc;
+        }
+        g->lr = r->gLr;
+        r->guide = g;
+    }
+    if (mode != r->guideMode) {
+        r->guideMode = mode;
+        r->graphDirty = true;
+    }
+    return ensureGuideBuffers(r);
+}
+
+int optpt_set_guiding_options(optpt_renderer *r, const optpt_guiding_options *o)
+{
+    if (!r || !o)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if (o->alphaMax < 0.0f || o->alphaMax >= 1.0f || o->alphaRamp < 0.0f || o->learningRate < 0.0f)
+        return fail(OPTPT_ERR_INVALID, "alphaMax must lie in [0, 1); alphaRamp and learningRate >= 0");
+    if (o->trainSteps > 64)
+        return fail(OPTPT_ERR_INVALID, "at most 64 training steps per pass");
+    if (o->trainSteps)
+        r->gTrainSteps = o->trainSteps;
+    if (o->trainStride)
+        r->gTrainStride = o->trainStride;
+    if (o->maxDepth)
+        r->gMaxDepth = o->maxDepth;
+    if (o->alphaMax > 0.0f)
+        r->gAlphaMax = o->alphaMax;
+    if (o->alphaRamp > 0.0f)
+        r->gAlphaRamp = o->alphaRamp;
+    if (o->learningRate > 0.0f) {
+        r->gLr = o->learningRate;
+        if (r->guide)
+            r->guide->lr = o->learningRate;
+    }
+    r->graphDirty = true;
+    return ensureGuideBuffers(r);
+}
+
+int optpt_get_guiding_options(const optpt_renderer *r, optpt_guiding_options *o)
+{
+    if (!r || !o)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    o->trainSteps = r->gTrainSteps;
+    o->trainStride = r->gTrainStride;
+    o->maxDepth = r->gMaxDepth;
+    o->alphaMax = r->gAlphaMax;
+    o->alphaRamp = r->gAlphaRamp;
+    o->learningRate = r->gLr;
+    return OPTPT_OK;
+}
+
+int optpt_guiding_batch(optpt_renderer *r, float *samples, uint32_t capacity, uint32_t *count)
+{
+    if (!r || !count)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    *count = 0;
+    if (!r->gBatchCount)
+        return OPTPT_OK;
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "guiding batch");
+    uint32_t n = 0;
+    CUDA_OR_RETURN(cudaMemcpy(&n, r->gBatchCount, sizeof(n), cudaMemcpyDeviceToHost), "guiding batch");
+    n = std::min(n, r->gBatchCap);
+    *count = n;
+    if (samples && capacity)
+        CUDA_OR_RETURN(cudaMemcpy(samples, r->gBatch, sizeof(GuideSample) * std::min(n, capacity),
+                                  cudaMemcpyDeviceToHost),
+                       "guiding batch");
+    return OPTPT_OK;
+}
+
+int optpt_get_guide(optpt_renderer *r, optpt_guide **out)
+{
+    if (!r || !out)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    *out = r->guide;
     return OPTPT_OK;
 }
 
@@ -636,9 +828,9 @@ int optpt_set_launch_params(optpt_renderer *r, const LaunchParams *lp)
     if (lp->toneMappingImpl != 0 && lp->toneMappingImpl != 1)
         return fail(OPTPT_ERR_INVALID, "toneMappingImpl must be 0 or 1");
     if (lp->sample != r->lp.sample) {
-        uint32_t st[4] = {lp->sample, 0, 0, 0};
+        const uint32_t st = lp->sample;  // state[1] (the pass count) runs on
         CUDA_OR_RETURN(cudaDeviceSynchronize(), "set sample");
-        CUDA_OR_RETURN(cudaMemcpy(r->dState, st, sizeof(st), cudaMemcpyHostToDevice), "set sample");
+        CUDA_OR_RETURN(cudaMemcpy(r->dState, &st, sizeof(st), cudaMemcpyHostToDevice), "set sample");
     }
     if (lp->maxDepth != r->lp.maxDepth)
         r->graphDirty = true;
@@ -670,6 +862,8 @@ int optpt_render(optpt_renderer *r, uint32_t spp, void *stream)
     // replay the captured graph; a remainder runs as one smaller pass.
     const FrameConst fc = r->frameConst();
     CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    if ((rc = ensureGuideBuffers(r)))
+        return rc;
     const uint32_t passes = spp / r->sppBatch, rem = spp % r->sppBatch;
     if (r->opt.useGraph && passes) {
         if ((rc = ensureGraph(r, st ? st : r->ownStream)))
@@ -726,7 +920,7 @@ int optpt_reset_sample_count(optpt_renderer *r)
     const size_t npix = (size_t)r->w * r->h;
     CUDA_OR_RETURN(cudaMemset(r->acc.sum, 0, sizeof(Acc4) * npix), "reset");
     CUDA_OR_RETURN(cudaMemset(r->acc.sumSq, 0, sizeof(Acc4) * npix), "reset");
-    CUDA_OR_RETURN(cudaMemset(r->dState, 0, sizeof(uint32_t) * 4), "reset");
+    CUDA_OR_RETURN(cudaMemset(r->dState, 0, sizeof(uint32_t)), "reset");
     r->lp.sample = 0;
     r->hostFbValid = false;
     return OPTPT_OK;
@@ -807,9 +1001,11 @@ int optpt_render_profiled(optpt_renderer *r, uint32_t spp, void *stream, optpt_k
     if (!out)
         return fail(OPTPT_ERR_INVALID, "NULL argument");
     memset(out, 0, sizeof(*out));
+    if ((rc = ensureGuideBuffers(r)))
+        return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const FrameParams fp = r->frameParams();
-    const int maxEv = 3 + 3 * (int)fp.maxDepth;
+    const int maxEv = 4 + 4 * (int)fp.maxDepth;
     std::vector<cudaEvent_t> ev(maxEv);
     std::vector<int> kind(maxEv);
     for (auto &e : ev)
@@ -826,13 +1022,13 @@ int optpt_render_profiled(optpt_renderer *r, uint32_t spp, void *stream, optpt_k
             pf.sppBatch = spp % r->sppBatch;
             pf.numPaths = r->w * r->h * pf.sppBatch;
         }
-        enqueuePass(r, pf, st, ev.data(), kind.data());
+        const int marks = enqueuePass(r, pf, st, ev.data(), kind.data());
         CUDA_OR_RETURN(cudaStreamSynchronize(st), "profile pass");
-        for (int k = 0; k + 1 < maxEv; ++k) {
+        for (int k = 0; k + 1 < marks; ++k) {
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
             out->ms[kind[k]] += ms;
-            out->launches[kind[k]] += kind[k] == 3 ? 2 : 1;
+            out->launches[kind[k]] += kind[k] == 3 ? 2 : kind[k] == 6 ? 1 + 5 * r->gTrainSteps : 1;
         }
     }
     r->lp.sample += spp;
@@ -852,6 +1048,8 @@ int optpt_traversal_counts(optpt_renderer *r, uint32_t spp, void *stream, optpt_
         return rc;
     if (!out)
         return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if ((rc = ensureGuideBuffers(r)))
+        return rc;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned long long before[8], after[8];
     const FrameConst fc = r->frameConst();

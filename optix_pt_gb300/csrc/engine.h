@@ -60,12 +60,47 @@ struct FrameConst {
     float4 bg;   // xyz
 };
 
+// Learned guiding inside a pass (all null / 0 when guiding is off).
+//   mix      : packed vMF mixture per queued extension ray (80 B), written by
+//              the inference kernel after each extend
+//   rec      : training records, GUIDE_REC float4 per (training path, depth)
+//   batch    : training samples gathered at the end of the pass
+struct GuidePass {
+    const void *mix;
+    float4 *rec;
+    void *batch;
+    uint32_t *batchCount;    // device
+    uint32_t on;             // 1: guided sampling at guidable vertices
+    uint32_t train;          // 1: record training vertices
+    uint32_t trainStride;    // every trainStride-th path is a training path
+    uint32_t batchCapacity;
+    const uint32_t *step;    // device: training steps taken so far
+    float alphaMax;          // probability of sampling the learned mixture once trained
+    float alphaRamp;         // that probability is alphaMax * min(1, steps / alphaRamp)
+    uint32_t maxDepth;       // vertices deeper than this sample the BSDF only
+};
+#define GUIDE_REC 7
+
+// Training paths: one per group of `stride` consecutive paths, at an offset
+// drawn per group and per pass, so every pixel contributes over passes.
+__host__ __device__ inline uint32_t guideTrainOffset(uint32_t group, uint32_t stamp, uint32_t stride)
+{
+    uint32_t h = group * 0x9E3779B1u ^ stamp * 0x85EBCA77u;
+    h ^= h >> 16;
+    h *= 0x7FEB352Du;
+    h ^= h >> 15;
+    h *= 0x846CA68Bu;
+    h ^= h >> 16;
+    return h % stride;
+}
+
 // Launch-shape parameters baked into a captured pass.
 struct FrameParams {
     uint32_t w, h, npix, sppBatch, numPaths;
     uint32_t maxDepth;
-    const uint32_t *state;   // device: [0] = samples accumulated before this pass
+    const uint32_t *state;   // device: [0] = samples accumulated before this pass, [1] = passes run
     const FrameConst *fc;    // device
+    GuidePass guide;
 };
 
 // Device counters: per-depth queue lengths. Depth d uses index d.
@@ -121,6 +156,12 @@ void launchAccumulate(const LaunchShape &ls, const FrameParams &fp, const WaveBu
 void launchAdvance(const FrameParams &fp, uint32_t *state, cudaStream_t st);
 void launchTrace(const DevScene &s, const float4 *rays, float4 *hits, uint32_t n, int anyHit, cudaStream_t st);
 void launchBsdfBatch(const void *queries, void *results, uint32_t n, cudaStream_t st);
+// guide.cu: inference over the extension queue of `depth` (after extend), and
+// the end-of-pass gather of training samples from the records.
+struct optpt_guide;
+void launchGuideInfer(const optpt_guide *g, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
+                      cudaStream_t st);
+void launchGuideGather(const FrameParams &fp, const WaveBufs &q, cudaStream_t st);
 int occupancyGrid(int kernelId, int block);  // persistent grid for a kernel class
 
 // bvh_build.cu, bvh8_build.cu

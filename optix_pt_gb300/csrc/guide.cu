@@ -23,6 +23,7 @@
 #include "optpt.h"
 #include "tc.cuh"
 #include "guide_net.h"
+#include "engine.h"
 
 extern "C" int optpt_internal_set_error(int code, const char *msg);
 
@@ -178,6 +179,35 @@ struct QueryInput {
         return true;
     }
     __device__ uint32_t count() const { return n; }
+    __device__ void resolve() {}
+};
+
+// Hits of the extension queue at one depth: position, face-forwarded
+// geometric normal and outgoing direction (the same inputs the shading
+// kernel records for training).
+struct HitInput {
+    const float4 *rayO, *rayD, *hit, *triV;
+    const uint32_t *countPtr;
+    uint32_t n;
+    __device__ bool fetch(uint32_t i, float3 &p, float3 &nrm, float3 &wo) const
+    {
+        if (i >= n)
+            return false;
+        const float4 h = hit[i];
+        const int leaf = __float_as_int(h.w);
+        if (leaf < 0)
+            return false;
+        const float3 o = f3of4(rayO[i]), d = f3of4(rayD[i]);
+        p = o + h.x * d;
+        const float3 v0 = f3of4(__ldg(&triV[3 * leaf])), v1 = f3of4(__ldg(&triV[3 * leaf + 1])),
+                     v2 = f3of4(__ldg(&triV[3 * leaf + 2]));
+        const float3 Ng = normalize3(cross3(v1 - v0, v2 - v0));
+        nrm = dot3(Ng, d) < 0.0f ? Ng : -Ng;
+        wo = -d;
+        return true;
+    }
+    __device__ uint32_t count() const { return n; }
+    __device__ void resolve() { n = *countPtr; }
 };
 
 constexpr uint32_t INFER_SMEM = LAYERS * W_BYTES + TILE_BYTES + 1024;
@@ -209,6 +239,7 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t tm = tmemBase;
     bool ok = __syncthreads_and(tc::mbarWait(&barLoad, 0) ? 1 : 0) != 0;
     Sync sync{&barMma, 0};
+    in.resolve();
     const uint32_t n = in.count();
     for (uint32_t base = blockIdx.x * TILE_ROWS; ok && base < n; base += gridDim.x * TILE_ROWS) {
         float3 p, nrm, wo;
@@ -292,12 +323,14 @@ __device__ void lossGradient(const float *o, float3 wi, float c, float *d, float
     }
 }
 
+constexpr double WEIGHT_CAP = 16.0;
 constexpr uint32_t TRAIN_SMEM = 2 * LAYERS * W_BYTES + LAYERS * TILE_BYTES + TILE_BYTES + 1024;
 constexpr uint32_t TRAIN_TMEM = 512;  // [0, 64) layer results; [64 + 64 l, 128 + 64 l) dW_l
 
 __global__ void __launch_bounds__(128, 1)
     kGuideTrain(GuideGeom g, const float *hash, const uint8_t *tiles, const GuideSample *smp, const uint32_t *countPtr,
-                uint32_t capacity, const double *stats, float *gMlp, float *gHash, double *lossOut, int *status)
+                uint32_t capacity, uint32_t slice, uint32_t slices, const double *stats, float *gMlp, float *gHash,
+                double *lossOut, int *status)
 {
     extern __shared__ uint8_t smRaw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smRaw) + 1023) & ~uintptr_t(1023));
@@ -324,18 +357,24 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t tm = tmemBase;
     bool ok = __syncthreads_and(tc::mbarWait(&barLoad, 0) ? 1 : 0) != 0;
     Sync sync{&barMma, 0};
-    const uint32_t n = min(*countPtr, capacity);
+    const uint32_t total = min(*countPtr, capacity);
+    const uint32_t b0 = (uint32_t)((uint64_t)total * slice / slices);
+    const uint32_t n = (uint32_t)((uint64_t)total * (slice + 1) / slices);
+    // weights are normalised by the batch sum and capped at WEIGHT_CAP times
+    // the mean positive weight: single-path radiance estimates are heavy
+    // tailed, and a handful of samples would otherwise steer a whole step
     const double wsum = stats[0];
     const float scale = wsum > 0.0 ? (float)(1.0 / wsum) : 0.0f;
+    const float cap = stats[3] > 0.0 ? (float)(WEIGHT_CAP * wsum / stats[3]) : 0.0f;
     bool firstTile = true;
     float lossAcc = 0.0f;
-    for (uint32_t base = blockIdx.x * TILE_ROWS; ok && base < n; base += gridDim.x * TILE_ROWS) {
+    for (uint32_t base = b0 + blockIdx.x * TILE_ROWS; ok && base < n; base += gridDim.x * TILE_ROWS) {
         const uint32_t i = base + t;
         const bool valid = i < n;
         GuideSample s{};
         if (valid)
             s = smp[i];
-        const float c = valid && isfinite(s.pos.w) && s.pos.w > 0.0f ? s.pos.w * scale : 0.0f;
+        const float c = valid && isfinite(s.pos.w) && s.pos.w > 0.0f ? fminf(s.pos.w, cap) * scale : 0.0f;
         encodeRow<false>(g, hash, nullptr, f3of4(s.pos), f3of4(s.n), f3of4(s.wo), valid, sX, t);
         float v[WIDTH];
         // forward
@@ -456,28 +495,89 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // Sum of finite positive sample weights and the sample count of the batch.
-__global__ void kBatchStats(const GuideSample *smp, const uint32_t *countPtr, uint32_t capacity, double *stats)
+__global__ void kBatchStats(const GuideSample *smp, const uint32_t *countPtr, uint32_t capacity, uint32_t slice,
+                            uint32_t slices, double *stats)
 {
-    const uint32_t n = min(*countPtr, capacity);
-    double acc = 0.0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t total = min(*countPtr, capacity);
+    const uint32_t b0 = (uint32_t)((uint64_t)total * slice / slices);
+    const uint32_t n = (uint32_t)((uint64_t)total * (slice + 1) / slices);
+    double acc = 0.0, pos = 0.0;
+    for (uint32_t i = b0 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float w = smp[i].pos.w;
-        if (isfinite(w) && w > 0.0f)
+        if (isfinite(w) && w > 0.0f) {
             acc += (double)w;
+            pos += 1.0;
+        }
     }
-    for (int off = 16; off > 0; off >>= 1)
+    for (int off = 16; off > 0; off >>= 1) {
         acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if ((threadIdx.x & 31) == 0 && acc != 0.0)
+        pos += __shfl_down_sync(0xffffffffu, pos, off);
+    }
+    if ((threadIdx.x & 31) == 0 && acc != 0.0) {
         atomicAdd(stats, acc);
+        atomicAdd(stats + 3, pos);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0)
-        atomicAdd(stats + 2, (double)n);
+        atomicAdd(stats + 2, (double)(n - b0));
+}
+
+// ------------------------------------------------------------------ training samples of a pass
+// For every complete record (vertex written at depth d, arrival snapshot at
+// d + 1, both in this pass): incident radiance Li = (L_final - L_arrival) /
+// T_arrival; target F = luminance(f cos * Li); weight = F / density of wi.
+__global__ void kGuideGather(FrameParams fp, WaveBufs q)
+{
+    const GuidePass gp = fp.guide;
+    const uint32_t stamp = __ldg(fp.state + 1) + 1u;
+    const uint32_t numTrain = (fp.numPaths + gp.trainStride - 1u) / gp.trainStride;
+    const uint32_t total = numTrain * fp.maxDepth;
+    GuideSample *batch = reinterpret_cast<GuideSample *>(gp.batch);
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const float4 *r = gp.rec + (size_t)idx * GUIDE_REC;
+        const float4 r1 = r[1], r5 = r[5];
+        if (__float_as_uint(r1.w) != stamp || __float_as_uint(r5.w) != stamp)
+            continue;
+        const uint32_t group = idx / fp.maxDepth;
+        const uint32_t path = group * gp.trainStride + guideTrainOffset(group, stamp, gp.trainStride);
+        if (path >= fp.numPaths)
+            continue;
+        const float3 Lf = f3of4(q.pathL[path]), Ls = f3of4(r5), Ta = f3of4(r[6]), fc = f3of4(r[4]);
+        const float3 dL = Lf - Ls;
+        const float3 Li = mk3(Ta.x > 0.0f ? dL.x / Ta.x : 0.0f, Ta.y > 0.0f ? dL.y / Ta.y : 0.0f,
+                              Ta.z > 0.0f ? dL.z / Ta.z : 0.0f);
+        const float F = 0.2126f * fc.x * Li.x + 0.7152f * fc.y * Li.y + 0.0722f * fc.z * Li.z;
+        const float4 r0 = r[0];
+        const float w = F / r0.w;
+        if (!(w > 0.0f) || !isfinite(w))
+            continue;
+        const uint32_t slot = atomicAdd(gp.batchCount, 1u);
+        if (slot >= gp.batchCapacity)
+            continue;
+        GuideSample smp;
+        smp.pos = make_float4(r0.x, r0.y, r0.z, w);
+        smp.n = r1;
+        smp.wo = r[2];
+        smp.wi = r[3];
+        batch[slot] = smp;
+    }
 }
 
 // ------------------------------------------------------------------ Adam
 constexpr float BETA1 = 0.9f, BETA2 = 0.99f, ADAM_EPS = 1e-15f;
 
-__global__ void kAdamHash(float *p, __half *ph, float *gr, float *m, float *v, size_t n, float lr, float c1, float c2)
+__global__ void kAdamStep(uint32_t *step) { *step += 1u; }
+
+__device__ __forceinline__ void biasCorrection(const uint32_t *step, float &c1, float &c2)
 {
+    const float t = (float)*step;
+    c1 = 1.0f / (1.0f - powf(BETA1, t));
+    c2 = 1.0f / (1.0f - powf(BETA2, t));
+}
+
+__global__ void kAdamHash(float *p, __half *ph, float *gr, float *m, float *v, size_t n, float lr, const uint32_t *step)
+{
+    float c1, c2;
+    biasCorrection(step, c1, c2);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const float g = gr[i];
         float mi = m[i], vi = v[i];
@@ -495,8 +595,10 @@ __global__ void kAdamHash(float *p, __half *ph, float *gr, float *m, float *v, s
 }
 
 // MLP weights: Adam, then both BF16 tile layouts.
-__global__ void kAdamMlp(float *p, uint8_t *tiles, float *gr, float *m, float *v, float lr, float c1, float c2)
+__global__ void kAdamMlp(float *p, uint8_t *tiles, float *gr, float *m, float *v, float lr, const uint32_t *step)
 {
+    float c1, c2;
+    biasCorrection(step, c1, c2);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MLP_PARAMS; i += gridDim.x * blockDim.x) {
         const float g = gr[i];
         const float mi = BETA1 * m[i] + (1.0f - BETA1) * g;
@@ -547,6 +649,8 @@ cudaError_t setSmem()
     cudaError_t e = cudaFuncSetAttribute(kGuideTrain, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(kGuideInfer<QueryInput>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kGuideInfer<HitInput>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
     done = e == cudaSuccess;
     return e;
 }
@@ -566,7 +670,7 @@ GuideGeom guideGeom(const optpt_guide *g)
 void guideFree(optpt_guide *g)
 {
     void *ptrs[] = {g->mlp, g->tiles, g->hash, g->hashH, g->gMlp, g->gHash, g->mMlp,
-                    g->vMlp, g->mHash, g->vHash, g->stats, g->status};
+                    g->vMlp, g->mHash, g->vHash, g->stats, g->status, g->dStep};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -608,6 +712,7 @@ int guideCreate(optpt_guide *g, const float lo[3], const float hi[3], uint32_t s
     alloc((void **)&g->vHash, sizeof(float) * HASH_PARAMS);
     alloc((void **)&g->stats, sizeof(double) * 4);
     alloc((void **)&g->status, sizeof(int));
+    alloc((void **)&g->dStep, sizeof(uint32_t));
     if (e != cudaSuccess) {
         guideFree(g);
         return optpt_internal_set_error(OPTPT_ERR_NOMEM, cudaGetErrorString(e));
@@ -655,28 +760,42 @@ cudaError_t guideInferQueries(const optpt_guide *g, const GuideQuery *q, uint32_
 }
 
 cudaError_t guideGradients(optpt_guide *g, const GuideSample *smp, const uint32_t *count, uint32_t capacity,
-                           cudaStream_t s)
+                           cudaStream_t s, uint32_t slice, uint32_t slices)
 {
     cudaError_t e = cudaMemsetAsync(g->stats, 0, sizeof(double) * 4, s);
     if (e != cudaSuccess)
         return e;
-    kBatchStats<<<g->numSMs, 256, 0, s>>>(smp, count, capacity, g->stats);
-    const int grid = std::min(g->numSMs, (int)((capacity + TILE_ROWS - 1) / TILE_ROWS));
+    kBatchStats<<<g->numSMs, 256, 0, s>>>(smp, count, capacity, slice, slices, g->stats);
+    const uint32_t perSlice = (capacity + slices - 1) / slices;
+    const int grid = std::min(g->numSMs, (int)((perSlice + TILE_ROWS - 1) / TILE_ROWS));
     if (grid > 0)
-        kGuideTrain<<<grid, 128, TRAIN_SMEM, s>>>(guideGeom(g), g->hash, g->tiles, smp, count, capacity, g->stats,
-                                                   g->gMlp, g->gHash, g->stats + 1, g->status);
+        kGuideTrain<<<grid, 128, TRAIN_SMEM, s>>>(guideGeom(g), g->hash, g->tiles, smp, count, capacity, slice, slices,
+                                                   g->stats, g->gMlp, g->gHash, g->stats + 1, g->status);
     return cudaGetLastError();
 }
 
 cudaError_t guideAdam(optpt_guide *g, cudaStream_t s)
 {
-    ++g->step;
-    const float c1 = 1.0f / (1.0f - std::pow(BETA1, (float)g->step));
-    const float c2 = 1.0f / (1.0f - std::pow(BETA2, (float)g->step));
-    kAdamMlp<<<20, 256, 0, s>>>(g->mlp, g->tiles, g->gMlp, g->mMlp, g->vMlp, g->lr, c1, c2);
-    kAdamHash<<<g->numSMs * 8, 256, 0, s>>>(g->hash, g->hashH, g->gHash, g->mHash, g->vHash, HASH_PARAMS, g->lr, c1,
-                                            c2);
+    kAdamStep<<<1, 1, 0, s>>>(g->dStep);
+    kAdamMlp<<<20, 256, 0, s>>>(g->mlp, g->tiles, g->gMlp, g->mMlp, g->vMlp, g->lr, g->dStep);
+    kAdamHash<<<g->numSMs * 8, 256, 0, s>>>(g->hash, g->hashH, g->gHash, g->mHash, g->vHash, HASH_PARAMS, g->lr,
+                                            g->dStep);
     return cudaGetLastError();
+}
+
+void launchGuideInfer(const optpt_guide *g, const DevScene &sc, const FrameParams &fp, const WaveBufs &q, int depth,
+                      cudaStream_t st)
+{
+    const int cur = depth & 1;
+    HitInput in{q.rayO[cur], q.rayD[cur], q.hit, sc.triV, q.counters + CNT_EXT + depth, 0u};
+    kGuideInfer<HitInput><<<g->numSMs * 3, 128, INFER_SMEM, st>>>(
+        guideGeom(g), g->hashH, g->tiles, in, reinterpret_cast<Packed *>(const_cast<void *>(fp.guide.mix)),
+        g->status);
+}
+
+void launchGuideGather(const FrameParams &fp, const WaveBufs &q, cudaStream_t st)
+{
+    kGuideGather<<<1024, 256, 0, st>>>(fp, q);
 }
 
 // ------------------------------------------------------------------ C ABI
@@ -802,7 +921,7 @@ int optpt_guide_train_step(optpt_guide *g, const float *samples, const uint32_t 
     return OPTPT_OK;
 }
 
-int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss)
+int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss, double *lastSamples)
 {
     if (!g || !status)
         return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
@@ -814,6 +933,8 @@ int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss)
         return optpt_internal_set_error(OPTPT_ERR_CUDA, cudaGetErrorString(e));
     if (lastLoss)
         *lastLoss = stats[1];
+    if (lastSamples)
+        *lastSamples = stats[2];
     return OPTPT_OK;
 }
 

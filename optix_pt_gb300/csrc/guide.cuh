@@ -14,12 +14,12 @@ namespace guide {
 constexpr int LEVELS = 16;            // hash-grid levels
 constexpr int FEATS = 2;              // features per level
 constexpr uint32_t TABLE = 1u << 19;  // entries per level
-constexpr float RES_MIN = 16.0f, RES_MAX = 1024.0f;
+constexpr float RES_MIN = 16.0f, RES_MAX = 256.0f;
 constexpr int WIDTH = 64;             // network width (inputs padded to 64)
 constexpr int LAYERS = 5;             // 64x64 weight matrices: in -> h1 -> h2 -> h3 -> h4 -> out
 constexpr int LOBES = 8;              // vMF lobes; outputs 5k..5k+4 = (mu raw xyz, log kappa, weight logit)
 constexpr int IN_NORMAL = 2 * LEVELS, IN_WO = IN_NORMAL + 3, IN_ONE = IN_WO + 3;
-constexpr float LOG_KAPPA_MIN = -3.0f, LOG_KAPPA_MAX = 8.0f;
+constexpr float LOG_KAPPA_MIN = -3.0f, LOG_KAPPA_MAX = 5.5f;
 constexpr size_t HASH_PARAMS = (size_t)LEVELS * TABLE * FEATS;
 constexpr int MLP_PARAMS = LAYERS * WIDTH * WIDTH;
 

@@ -18,7 +18,7 @@ struct optpt_guide {
     float *mMlp = nullptr, *vMlp = nullptr, *mHash = nullptr, *vHash = nullptr;
     double *stats = nullptr;  // [0] sum of normalised weights, [1] loss sum, [2] samples
     int *status = nullptr;    // device: non-zero if a tensor-core wait expired
-    uint32_t step = 0;
+    uint32_t *dStep = nullptr;  // device: Adam step count
     float lr = 1e-2f;
     int numSMs = 0;
 };
@@ -48,6 +48,7 @@ GuideGeom guideGeom(const optpt_guide *g);
 cudaError_t guideInferQueries(const optpt_guide *g, const GuideQuery *q, uint32_t n, guide::Packed *out,
                               cudaStream_t s);
 // Gradients of the batch into gMlp / gHash (accumulated; zeroed by Adam).
+// Slice `slice` of `slices` equal parts of the batch (one minibatch).
 cudaError_t guideGradients(optpt_guide *g, const GuideSample *smp, const uint32_t *count, uint32_t capacity,
-                           cudaStream_t s);
+                           cudaStream_t s, uint32_t slice = 0, uint32_t slices = 1);
 cudaError_t guideAdam(optpt_guide *g, cudaStream_t s);

@@ -582,12 +582,16 @@ int buildTerrain(uint32_t seed, int grid, int rocks, int texRes, optpt_scene *ou
 }
 
 // Indirect-lit interior: a closed 10 x 4 x 6 room (x in [-5, 5], y in [0, 4],
-// z in [-3, 3]) whose only opening is a 1 x 2 doorway in the x = +5 wall; a
-// 3 x 3 quad emitter of radiance 50 stands outside, facing the doorway, and
-// the background is black, so everything inside is lit through the doorway.
-// Furniture: tables and chairs of boxes, shelves, and `balls` icospheres of
-// `subdiv` levels on the floor, table tops and shelves; materials are diffuse
-// (roughness 1, no specular lobe) or GGX metal (roughness U(0.1, 0.6)).
+// z in [-3, 3]) whose only opening is a 1 x 2 doorway (z in [-0.5, 0.5],
+// y in [0, 2]) through a 0.1-thick wall at x = 5. Outside, a 2 x 2 quad
+// emitter of radiance 50 hangs on the outer face of that wall beside the
+// doorway, facing away from the house, onto an outside ground and a bounce
+// wall at x = 9. No point inside sees the emitter's front: everything inside
+// is lit indirectly, through the doorway (next-event estimation finds no
+// light from inside). The background is black. Furniture: tables and chairs
+// of boxes, shelves, and `balls` icospheres of `subdiv` levels on the floor,
+// table tops and shelves; materials are diffuse (roughness 1, no specular
+// lobe) or GGX metal (roughness U(0.1, 0.6)).
 int buildInterior(uint32_t seed, int balls, int subdiv, optpt_scene *out)
 {
     Builder b;
@@ -602,6 +606,9 @@ int buildInterior(uint32_t seed, int balls, int subdiv, optpt_scene *out)
     MaterialData light = baseMaterial(0.0, 0.0, 0.0);
     setv(light.emission, 50.0, 50.0, 50.0);
     const int lightM = b.addMaterial(light);
+    MaterialData outside = baseMaterial(0.8, 0.78, 0.74);
+    outside.specular = 0.0f;
+    const int outM = b.addMaterial(outside);
     std::vector<int> furnM;
     for (int k = 0; k < 16; ++k) {
         MaterialData m = baseMaterial(rng.range(0.2, 0.9), rng.range(0.2, 0.9), rng.range(0.2, 0.9));
@@ -615,18 +622,28 @@ int buildInterior(uint32_t seed, int balls, int subdiv, optpt_scene *out)
     }
     auto pick = [&]() { return furnM[(size_t)(rng.uniform() * furnM.size()) % furnM.size()]; };
 
-    const double X = 5.0, Y = 4.0, Z = 3.0, dz = 0.5, dy = 2.0;
+    const double X = 5.0, Y = 4.0, Z = 3.0, dz = 0.5, dy = 2.0, T = 0.1, XO = X + T;
     b.quad({-X, 0, -Z}, {X, 0, -Z}, {X, 0, Z}, {-X, 0, Z}, {0, 1, 0}, floorM);      // floor
     b.quad({-X, Y, -Z}, {X, Y, -Z}, {X, Y, Z}, {-X, Y, Z}, {0, -1, 0}, wallM);      // ceiling
     b.quad({-X, 0, -Z}, {X, 0, -Z}, {X, Y, -Z}, {-X, Y, -Z}, {0, 0, 1}, wallM);     // back (z = -3)
     b.quad({-X, 0, Z}, {X, 0, Z}, {X, Y, Z}, {-X, Y, Z}, {0, 0, -1}, wallM);        // front (z = +3)
     b.quad({-X, 0, -Z}, {-X, 0, Z}, {-X, Y, Z}, {-X, Y, -Z}, {1, 0, 0}, wallM);     // x = -5
-    // x = +5 wall around the doorway z in [-0.5, 0.5], y in [0, 2]
-    b.quad({X, 0, -Z}, {X, 0, -dz}, {X, Y, -dz}, {X, Y, -Z}, {-1, 0, 0}, wallM);
-    b.quad({X, 0, dz}, {X, 0, Z}, {X, Y, Z}, {X, Y, dz}, {-1, 0, 0}, wallM);
-    b.quad({X, dy, -dz}, {X, dy, dz}, {X, Y, dz}, {X, Y, -dz}, {-1, 0, 0}, wallM);
-    // outside: the emitter, facing the doorway
-    b.quad({X + 2.5, 0.0, -1.5}, {X + 2.5, 0.0, 1.5}, {X + 2.5, 3.0, 1.5}, {X + 2.5, 3.0, -1.5}, {-1, 0, 0}, lightM);
+    // the door wall, inner face (x = 5) and outer face (x = 5.1) around the
+    // doorway, and the doorway's jambs and lintel
+    for (double x : {X, XO}) {
+        const Vec f{x == X ? -1.0 : 1.0, 0, 0};
+        b.quad({x, 0, -Z}, {x, 0, -dz}, {x, Y, -dz}, {x, Y, -Z}, f, wallM);
+        b.quad({x, 0, dz}, {x, 0, Z}, {x, Y, Z}, {x, Y, dz}, f, wallM);
+        b.quad({x, dy, -dz}, {x, dy, dz}, {x, Y, dz}, {x, Y, -dz}, f, wallM);
+    }
+    b.quad({X, 0, -dz}, {XO, 0, -dz}, {XO, dy, -dz}, {X, dy, -dz}, {0, 0, 1}, wallM);
+    b.quad({X, 0, dz}, {XO, 0, dz}, {XO, dy, dz}, {X, dy, dz}, {0, 0, -1}, wallM);
+    b.quad({X, dy, -dz}, {XO, dy, -dz}, {XO, dy, dz}, {X, dy, dz}, {0, -1, 0}, wallM);
+    // outside: ground, bounce wall, and the emitter on the outer wall beside the door
+    b.quad({XO, 0, -Z}, {9.0, 0, -Z}, {9.0, 0, Z}, {XO, 0, Z}, {0, 1, 0}, outM);
+    b.quad({9.0, 0, -Z}, {9.0, 0, Z}, {9.0, Y, Z}, {9.0, Y, -Z}, {-1, 0, 0}, outM);
+    b.quad({XO + 0.02, 0.3, 0.8}, {XO + 0.02, 0.3, 2.8}, {XO + 0.02, 2.3, 2.8}, {XO + 0.02, 2.3, 0.8}, {1, 0, 0},
+           lightM);
 
     // tables (top + 4 legs) with chairs, keeping a lane from the doorway clear
     std::vector<Vec> tops;

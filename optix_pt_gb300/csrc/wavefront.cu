@@ -15,6 +15,7 @@
 #include "texture.cuh"
 #include "trace.cuh"
 #include "bvh8.cuh"
+#include "guide.cuh"
 
 // The traversal kernels are compiled for 4 resident 256-thread blocks per SM
 // (64 registers per thread): the extra warps hide node-fetch latency better
@@ -241,6 +242,9 @@ OPT_D float4 texAt(const DevScene &s, int tex, float4 tf, float2 tc)
 
 // Closest-hit shading, next-event estimation and continuation
 // (cu/path_tracer.cu:17-582), miss (cu/device_programs.cu:168-174).
+// GUIDED: the learned-guiding variant (mixture sampling and training
+// records); the plain variant carries none of that code.
+template <bool GUIDED>
 __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBufs q, int depth)
 {
     const uint32_t count = q.counters[CNT_EXT + depth];
@@ -255,6 +259,10 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
     float4 *const nextQ[2] = {q.rayO[nxt], q.rayD[nxt]};
     float4 *const shPQ[3] = {q.shO[0], q.shD[0], q.shC[0]};
     float4 *const shEQ[3] = {q.shO[1], q.shD[1], q.shC[1]};
+    // guide selection probability: ramps in with training (any value keeps
+    // the estimator unbiased; an untrained proposal should be used sparingly)
+    const float alpha =
+        GUIDED ? fp.guide.alphaMax * fminf(1.0f, (float)__ldg(fp.guide.step) / fp.guide.alphaRamp) : 0.0f;
 
     for (uint32_t base = warpId * 32u; base < count; base += nWarps * 32u) {
         const uint32_t i = base + (uint32_t)lane;
@@ -270,6 +278,20 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
             uint32_t flags = __float_as_uint(T4.w);
             const float3 rayDir = f3of4(rd), rayOrig = f3of4(ro);
             const int leaf = __float_as_int(hrec.w);
+            // Guiding: a training path's previous vertex learns the radiance
+            // and throughput on arrival here (everything added from now on
+            // arrived along its sampled direction).
+            const GuidePass &gp = fp.guide;
+            const uint32_t stamp = __ldg(fp.state + 1) + 1u;
+            float4 *rec = nullptr;
+            if (GUIDED && gp.train &&
+                path % gp.trainStride == guideTrainOffset(path / gp.trainStride, stamp, gp.trainStride))
+                rec = gp.rec + (size_t)(path / gp.trainStride) * fp.maxDepth * GUIDE_REC;
+            if (rec && depth > 1) {
+                float4 *r = rec + (size_t)(depth - 2) * GUIDE_REC;
+                r[5] = mk4(L, __uint_as_float(stamp));
+                r[6] = mk4(T, 0.0f);
+            }
             if (leaf < 0) {
                 L = L + bg * T;
             } else {
@@ -481,11 +503,44 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
                             smp.dir = mk3s(0.0f);
                             smp.bsdf = mk3s(0.0f);
                             smp.pdf = 0.0f;
-                            bsdf::sampleBrdf(m, wo, xi, U, smp);
-                            smp.pdf *= cw;
-                            if (!(smp.pdf < OPT_SCENE_EPSILON || maxc3(smp.bsdf) < OPT_SCENE_EPSILON)) {
-                                T = T * (smp.bsdf * fabsf(dot3(normal, smp.dir)) / smp.pdf);
-                                const float maxC = maxc3(T);
+                            const bool guided =
+                                GUIDED && (uint32_t)depth <= fp.guide.maxDepth && bsdf::guidable(cat);
+                            float pSample;  // density wi was drawn from (category chosen)
+                            float pcLobe = 0.0f;  // the lobe's own density at wi (guided vertices)
+                            bool live;
+                            if (guided) {
+                                // One-sample MIS of the learned mixture and the lobe's own
+                                // sampler. The lobe's density decides the kill test, as in
+                                // the plain estimator, so both integrate over the same set.
+                                guide::Mixture gm;
+                                guide::unpack(reinterpret_cast<const guide::Packed *>(gp.mix)[i], gm);
+                                const float uSel = U.next();
+                                if (uSel < alpha)
+                                    smp.dir = guide::mixtureSample(gm, xi.x, 1.0f - xi.y, xi.z);
+                                else
+                                    bsdf::sampleBrdf(m, wo, xi, U, smp);
+                                const float pc = bsdf::lobePdf(m, smp.dir, wo);
+                                pcLobe = pc;
+                                smp.bsdf = bsdf::lobeValue(m, smp.dir, wo);
+                                pSample = alpha * guide::mixturePdf(gm, smp.dir) + (1.0f - alpha) * fmaxf(pc, 0.0f);
+                                smp.pdf = pSample * cw;
+                                live = !(pc * cw < OPT_SCENE_EPSILON || maxc3(smp.bsdf) < OPT_SCENE_EPSILON) &&
+                                       pSample > 0.0f;
+                            } else {
+                                bsdf::sampleBrdf(m, wo, xi, U, smp);
+                                pSample = smp.pdf;
+                                smp.pdf *= cw;
+                                live = !(smp.pdf < OPT_SCENE_EPSILON || maxc3(smp.bsdf) < OPT_SCENE_EPSILON);
+                            }
+                            if (live) {
+                                const float3 fcos = smp.bsdf * fabsf(dot3(normal, smp.dir));
+                                // Russian roulette reads the plain estimator's throughput for
+                                // this direction at guided vertices: a well-guided sample has a
+                                // small throughput because its density is high, and must not be
+                                // rouletted for it (any survival probability is unbiased).
+                                const float maxC = guided ? maxc3(T * (fcos / (cw * fmaxf(pcLobe, 1e-30f))))
+                                                          : maxc3(T * (fcos / smp.pdf));
+                                T = T * (fcos / smp.pdf);
                                 bool alive = true;
                                 if (depth > 3 || maxC < 0.3f) {
                                     const float qq = fmaxf(0.05f, 1.0f - maxC);
@@ -501,6 +556,17 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
                                     cont = true;
                                     nxtRay[0] = mk4(origin, __int_as_float((int)path));
                                     nxtRay[1] = mk4(smp.dir, 0.0f);
+                                    if (rec && guided) {
+                                        // the inference kernel's inputs: hit point, face-forwarded
+                                        // geometric normal, outgoing direction
+                                        float4 *r = rec + (size_t)(depth - 1) * GUIDE_REC;
+                                        const float3 nIn = dot3(Ng, rayDir) < 0.0f ? Ng : -Ng;
+                                        r[0] = mk4(rayOrig + hrec.x * rayDir, pSample);
+                                        r[1] = mk4(nIn, __uint_as_float(stamp));
+                                        r[2] = mk4(wo, 0.0f);
+                                        r[3] = mk4(smp.dir, 0.0f);
+                                        r[4] = mk4(fcos, 0.0f);
+                                    }
                                 }
                             }
                         }
@@ -622,7 +688,13 @@ __global__ void __launch_bounds__(256) kAccumulate(FrameParams fp, WaveBufs q, A
 }
 
 // Advances the sample counter after a pass (one thread).
-__global__ void kAdvance(uint32_t *state, uint32_t by) { state[0] += by; }
+// state[0]: samples accumulated (reset with the accumulator); state[1]: passes
+// run by this renderer (never reset; stamps guiding records).
+__global__ void kAdvance(uint32_t *state, uint32_t by)
+{
+    state[0] += by;
+    state[1] += 1u;
+}
 
 // ------------------------------------------------------------------ parity entry points
 __global__ void kTrace(DevScene s, const float4 *rays, float4 *hits, uint32_t n, int anyHit)
@@ -741,7 +813,10 @@ void launchExtend(const LaunchShape &ls, const DevScene &s, const FrameParams &f
 void launchShade(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                  cudaStream_t st)
 {
-    kShade<<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
+    if (fp.guide.on)
+        kShade<true><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
+    else
+        kShade<false><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
 }
 void launchShadow(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                   int which, cudaStream_t st, bool count)
@@ -786,7 +861,7 @@ int occupancyGrid(int kernelId, int block)
     switch (kernelId) {
     case 0: fn = (const void *)kGenerate; break;
     case 1: fn = (const void *)kExtend<false, true>; break;
-    case 2: fn = (const void *)kShade; break;
+    case 2: fn = (const void *)kShade<false>; break;
     case 3: fn = (const void *)kShadow<false, true>; break;
     case 11: fn = (const void *)kExtend<false, false>; break;
     case 13: fn = (const void *)kShadow<false, false>; break;

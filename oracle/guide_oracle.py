@@ -11,8 +11,8 @@ GPU implements, used to check its forward pass and gradients.
   BF16 operands with FP32 accumulation: every matrix operand is rounded to
   BF16 (round to nearest even) exactly where the tensor-core kernels round.
 * Output: 8 von Mises-Fisher lobes (mu = normalise(raw), kappa =
-  exp(clamp(raw, -3, 8)), weights = softmax(logits)); loss -c log q(wi) with
-  c = sample weight / sum of weights (Dong et al., "Neural Parametric
+  exp(clamp(raw, -3, 5.5)), weights = softmax(logits)); loss -c log q(wi) with
+  c = min(weight, 16 x mean positive weight) / sum of weights (Dong et al., "Neural Parametric
   Mixtures for Path Guiding", SIGGRAPH 2023), gradient in closed form.
 
 `gradients(..., use_bf16=False)` gives the exact FP64 gradient of the same loss,
@@ -22,7 +22,8 @@ import numpy as np
 
 LEVELS, FEATS, TABLE, WIDTH, LAYERS, LOBES = 16, 2, 1 << 19, 64, 5, 8
 IN_NORMAL, IN_WO, IN_ONE = 32, 35, 38
-LOG_KAPPA_MIN, LOG_KAPPA_MAX = -3.0, 8.0
+LOG_KAPPA_MIN, LOG_KAPPA_MAX = -3.0, 5.5
+WEIGHT_CAP = 16.0
 
 
 def bf16(x):
@@ -168,7 +169,8 @@ def gradients(mlp, hash_params, geom, samples, use_bf16=True):
     wgt = s[:, 3].astype(np.float64)
     ok = np.isfinite(wgt) & (wgt > 0)
     total = wgt[ok].sum()
-    c = np.where(ok, wgt / total if total > 0 else 0.0, 0.0)
+    cap = np.float32(WEIGHT_CAP * total / max(ok.sum(), 1))   # heavy-tail cap, as the kernel applies it
+    c = np.where(ok, np.minimum(s[:, 3], cap).astype(np.float64) / total if total > 0 else 0.0, 0.0)
     ent, wts = corners(res, dense, lo, inv_ext, s[:, 0:3])
     x0 = encode(hash_params, ent, wts, s[:, 4:7], s[:, 8:11], np.float32 if use_bf16 else np.float64)
     xs, z = forward(mlp, x0, use_bf16)

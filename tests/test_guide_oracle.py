@@ -12,7 +12,7 @@ def test_output_gradient_matches_finite_differences():
 
 
 def _geom():
-    res = np.floor(16.0 * (1024.0 / 16.0) ** (np.arange(16) / 15.0)).astype(np.float32)
+    res = np.floor(16.0 * (256.0 / 16.0) ** (np.arange(16) / 15.0)).astype(np.float32)
     dense = ((res + 1) ** 3 <= (1 << 19)).astype(np.uint32)
     return res, dense, np.zeros(3, np.float32), np.full(3, 0.1, np.float32)
 
