@@ -38,6 +38,12 @@ WORKLOADS = {
                 "scene": "terrain", "width": 1920, "height": 1080, "max_depth": 16, "spp_per_step": 1},
 }
 CPU_SPP = {"sweep": 36, "terrain": 32}  # CPU-baseline sample: about 10-30 s of host work
+# Learned guiding vs plain at equal wall time (the headline's second half):
+# the indirect-lit interior (1,947,146 tris) at a reduced resolution, against
+# a 65,536-spp plain FP64-accumulated reference of the same frame.
+GUIDED = {"workload": "indirect-lit interior (doorway only), 1,947,146 tris, depth 12",
+          "scene": "interior", "width": 320, "height": 180, "reference_spp": 65536, "budget_s": 2.0,
+          "seeds": [11, 12, 13]}
 WORKLOAD = dict(WORKLOADS["sweep"])
 METRIC = "Mrays/s (extension + shadow rays traced), progressive path tracing, 1 spp per step"
 NODE_BYTES = {8: 80, 2: 64}  # compressed BVH8 node, BVH2 node
@@ -136,6 +142,63 @@ def _camera_basis(eye, target, up, fov, aspect):
     V /= np.linalg.norm(V)
     vl = np.tan(0.5 * np.radians(fov))
     return list((U * vl * aspect).astype(np.float32)), list((V * vl).astype(np.float32)), list(W.astype(np.float32))
+
+
+def guided_equal_time(stream):
+    """relMSE (mean over pixels of sum_c (I - R)^2 / (R^2 + 1e-2)) of plain and
+    guided renders given the same wall-clock budget, online training included
+    in the guided budget; per seed a fresh renderer (and network)."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    g = GUIDED
+    scene = opt.Scene.procedural(g["scene"])
+    w, h = g["width"], g["height"]
+
+    def make(seed, mode):
+        r = opt.Renderer(scene)
+        r.setupOutputBuffer(w, h)
+        r.set_seed(seed)
+        if mode:
+            r.set_guiding(mode)
+        return r
+
+    t0 = time.perf_counter()
+    ref = make(1000, 0)
+    ref.render(g["reference_spp"], stream)
+    torch.cuda.synchronize()
+    s, _, n = ref.accum()
+    R = s.reshape(-1, 3) / n
+    ref_seconds = time.perf_counter() - t0
+    ref.close()
+    out = {}
+    for mode, name in ((0, "plain"), (1, "guided")):
+        errs, spps, mrays = [], [], []
+        for seed in g["seeds"]:
+            r = make(seed, mode)
+            batch = r.stats()["sppBatch"]
+            st0 = r.stats()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            spp = 0
+            while time.perf_counter() - t0 < g["budget_s"]:
+                r.render(batch, stream)
+                torch.cuda.synchronize()
+                spp += batch
+            dt = time.perf_counter() - t0
+            st1 = r.stats()
+            s, _, n = r.accum()
+            I = s.reshape(-1, 3) / n
+            errs.append(float(np.mean(((I - R) ** 2 / (R ** 2 + 1e-2)).sum(1))))
+            spps.append(spp)
+            mrays.append((st1["extensionRays"] - st0["extensionRays"] + st1["shadowRays"] - st0["shadowRays"]) / dt / 1e6)
+            r.close()
+        out[name] = {"relmse": float(np.mean(errs)), "relmse_per_seed": errs, "spp_in_budget": spps,
+                     "mrays_per_s": float(np.mean(mrays))}
+    out["relmse_ratio_plain_over_guided"] = out["plain"]["relmse"] / out["guided"]["relmse"]
+    out["config"] = dict(GUIDED, reference_seconds=ref_seconds,
+                         protocol="equal wall time per seed, online training inside the guided budget")
+    return out
 
 
 def run_reference(args, rank, world):
@@ -293,6 +356,10 @@ def run_ours(args, rank, world, local_rank):
                 "kernel_ms_per_pass": {k: v / 2 for k, v in kms.items()},
                 "kernel_share": {k: v / sum(kms.values()) for k, v in kms.items()}}
 
+    guided = None
+    if world == 1 and not args.no_guided:
+        guided = guided_equal_time(stream)
+
     # CPU baseline: the oracle integrator on this host's cores, bounded band.
     cpu = None
     if world == 1 and not args.no_cpu:
@@ -313,7 +380,8 @@ def run_ours(args, rank, world, local_rank):
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": 80,
                     "d2h_bytes_per_step": w * h * 16},
             "gpu_launches": passes_launches * args.steps,
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "guided_vs_plain_equal_time": guided}
     print(json.dumps(line))
     r.close()
 
@@ -327,6 +395,7 @@ def main():
     ap.add_argument("--workload", default="sweep", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-spp", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain equal-time comparison")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8])
     ap.add_argument("--leaf-size", type=int, default=0)
     ap.add_argument("--block-size", type=int, default=0)

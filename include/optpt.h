@@ -259,13 +259,19 @@ int optpt_guide_params(optpt_guide *g, float *mlp, float *hash, int write);
 int optpt_guide_levels(optpt_guide *g, float *res, uint32_t *dense, float *lo, float *invExt);
 
 /* Mixtures for n shading points. Device arrays: queries = 3 float4 each
- * (position, normal, outgoing direction; w ignored); mixtures = 80 bytes
- * each: per lobe (mu.xyz, kappa) as 4 halves, then the 8 weights as halves. */
+ * (position, normal, outgoing direction; w ignored); mixtures = 96 bytes
+ * each, as halves: per lobe (mu.xyz, kappa), then the 8 weights, then the
+ * probability of sampling the mixture rather than the BSDF, then 7 zeros. */
 int optpt_guide_infer(optpt_guide *g, const float *queries, uint32_t n, void *mixtures, void *stream);
 
-/* Gradient of the batch loss sum_i -c_i log q(wi_i), c_i = min(weight_i, 16 *
- * mean positive weight) / sum of weights. Device arrays: samples = 4 float4 each ((position, weight),
- * normal, outgoing, incoming direction wi); *count (device) = samples used,
+/* Gradient of the batch loss: for the selection probability a (a learned
+ * output), sum_i -c_i log(a q(wi_i) + (1 - a) pb_i), the density of the
+ * proposal the renderer samples; for the mixture q, sum_i -c_i log q(wi_i)
+ * (it learns the whole target). pb_i = the BSDF lobe's density at wi_i,
+ * c_i = min(weight_i, 16 * mean positive weight) / sum of weights. The
+ * reported loss is the first sum.
+ * Device arrays: samples = 4 float4 each ((position, weight), normal,
+ * (outgoing, pb), incoming direction wi); *count (device) = samples used,
  * at most `capacity`. Host outputs (NULL to skip): dMlp (5 x 64 x 64), dHash
  * (16 x 2^19 x 2), loss. Synchronises `stream`. */
 int optpt_guide_gradients(optpt_guide *g, const float *samples, const uint32_t *count, uint32_t capacity,
@@ -284,25 +290,35 @@ int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss, double *la
  * mode 0: plain BSDF sampling (bit-identical to a renderer that never had
  * guiding); 1: at guidable vertices (non-specular metal, diffuse, rough
  * reflection and coat lobes) the direction comes from the network's mixture
- * with probability 1/2, else from the BSDF, weighted by the one-sample MIS
- * density, and the network trains online after every pass on the pass's own
- * radiance estimates; 2: guided sampling with the network frozen. The
- * network is created on first use over the scene's bounding box. */
+ * with the network's selection probability, else from the BSDF, weighted by
+ * the one-sample MIS density; Russian roulette reads the plain estimator's
+ * throughput there; the network trains online after every pass on the
+ * pass's own radiance estimates; 2: guided sampling with the network frozen.
+ * The network is created on first use over the scene's bounding box. */
 int optpt_set_guiding(optpt_renderer *r, int mode);
 /* Guiding controls (0 / 0.0 fields keep the current value):
  * trainSteps   Adam steps per pass, each on one slice of the pass's samples (4)
  * trainStride  one path in trainStride records training samples (1)
  * maxDepth     vertices up to this depth are guided (all)
- * alphaMax     probability of sampling the network's mixture (0.5) ...
- * alphaRamp    ... reached after this many training steps, linearly (64)
- * learningRate Adam step size (1e-2) */
+ * alphaMin     floor (0) and
+ * alphaMax     cap (0.9) on the probability of sampling the network's
+ *              mixture instead of the BSDF; between them that probability is
+ *              the network's own (a learned output), phased in linearly ...
+ * alphaRamp    ... over this many training steps (64)
+ * learningRate Adam step size (1e-2)
+ * lobeLoss     1: the lobes learn the part of the target the BSDF leaves
+ *              (the loss of the whole proposal); 2: the whole target (2);
+ *              the selection probability always learns from the loss of the
+ *              whole proposal */
 typedef struct optpt_guiding_options {
     uint32_t trainSteps;
     uint32_t trainStride;
     uint32_t maxDepth;
+    float alphaMin;
     float alphaMax;
     float alphaRamp;
     float learningRate;
+    int32_t lobeLoss;
 } optpt_guiding_options;
 int optpt_set_guiding_options(optpt_renderer *r, const optpt_guiding_options *o);
 int optpt_get_guiding_options(const optpt_renderer *r, optpt_guiding_options *o);

@@ -296,7 +296,8 @@ class Renderer:
 
     def guiding_options(self, **kw):
         """Reads, and with keyword arguments updates, the guiding controls
-        (trainSteps, trainStride, maxDepth, alphaMax, alphaRamp, learningRate)."""
+        (trainSteps, trainStride, maxDepth, alphaMin, alphaMax, alphaRamp,
+        learningRate, lobeLoss)."""
         o = _ffi.GuidingOptions()
         if kw:
             for k, v in kw.items():

@@ -93,7 +93,8 @@ struct optpt_renderer {
     uint32_t *gBatchCount = nullptr;
     size_t gMixPaths = 0, gRecSlots = 0;
     uint32_t gTrainStride = 1, gBatchCap = 1u << 18, gTrainSteps = 4, gMaxDepth = 0xFFFFFFFFu;
-    float gAlphaMax = 0.5f, gAlphaRamp = 64.0f, gLr = 1e-2f;
+    float gAlphaMin = 0.0f, gAlphaMax = 0.9f, gAlphaRamp = 64.0f, gLr = 1e-2f;
+    int gLobeLoss = 1;
     float sceneLo[3] = {0, 0, 0}, sceneHi[3] = {0, 0, 0};
 
     FrameParams frameParams() const
@@ -117,6 +118,7 @@ struct optpt_renderer {
             fp.guide.trainStride = gTrainStride;
             fp.guide.batchCapacity = gBatchCap;
             fp.guide.step = guide->dStep;
+            fp.guide.alphaMin = gAlphaMin;
             fp.guide.alphaMax = gAlphaMax;
             fp.guide.alphaRamp = gAlphaRamp;
             fp.guide.maxDepth = gMaxDepth;
@@ -703,6 +705,7 @@ int optpt_set_guiding(optpt_renderer *r, int mode)
             return rc;
         }
         g->lr = r->gLr;
+        g->lobeLoss = r->gLobeLoss;
         r->guide = g;
     }
     if (mode != r->guideMode) {
@@ -716,8 +719,17 @@ int optpt_set_guiding_options(optpt_renderer *r, const optpt_guiding_options *o)
 {
     if (!r || !o)
         return fail(OPTPT_ERR_INVALID, "NULL argument");
-    if (o->alphaMax < 0.0f || o->alphaMax >= 1.0f || o->alphaRamp < 0.0f || o->learningRate < 0.0f)
-        return fail(OPTPT_ERR_INVALID, "alphaMax must lie in [0, 1); alphaRamp and learningRate >= 0");
+    if (o->alphaMax < 0.0f || o->alphaMax >= 1.0f || o->alphaMin < 0.0f || o->alphaMin >= 1.0f ||
+        o->alphaRamp < 0.0f || o->learningRate < 0.0f || o->lobeLoss < 0 || o->lobeLoss > 2)
+        return fail(OPTPT_ERR_INVALID, "alphaMin, alphaMax must lie in [0, 1); alphaRamp, learningRate >= 0; "
+                                       "lobeLoss 0, 1 or 2");
+    if (o->alphaMin > 0.0f)
+        r->gAlphaMin = o->alphaMin;
+    if (o->lobeLoss) {
+        r->gLobeLoss = o->lobeLoss - 1;
+        if (r->guide)
+            r->guide->lobeLoss = r->gLobeLoss;
+    }
     if (o->trainSteps > 64)
         return fail(OPTPT_ERR_INVALID, "at most 64 training steps per pass");
     if (o->trainSteps)
@@ -746,7 +758,9 @@ int optpt_get_guiding_options(const optpt_renderer *r, optpt_guiding_options *o)
     o->trainSteps = r->gTrainSteps;
     o->trainStride = r->gTrainStride;
     o->maxDepth = r->gMaxDepth;
+    o->alphaMin = r->gAlphaMin;
     o->alphaMax = r->gAlphaMax;
+    o->lobeLoss = r->gLobeLoss + 1;
     o->alphaRamp = r->gAlphaRamp;
     o->learningRate = r->gLr;
     return OPTPT_OK;

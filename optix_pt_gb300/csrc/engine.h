@@ -75,8 +75,9 @@ struct GuidePass {
     uint32_t trainStride;    // every trainStride-th path is a training path
     uint32_t batchCapacity;
     const uint32_t *step;    // device: training steps taken so far
-    float alphaMax;          // probability of sampling the learned mixture once trained
-    float alphaRamp;         // that probability is alphaMax * min(1, steps / alphaRamp)
+    float alphaMin;          // floor on the probability of sampling the learned mixture
+    float alphaMax;          // cap on the probability of sampling the learned mixture
+    float alphaRamp;         // that probability is min(alphaMax, min(1, steps / alphaRamp) * network's)
     uint32_t maxDepth;       // vertices deeper than this sample the BSDF only
 };
 #define GUIDE_REC 7

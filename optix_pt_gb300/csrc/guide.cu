@@ -285,8 +285,12 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ------------------------------------------------------------------ training
-// Gradient of -c log q(wi) w.r.t. the 40 raw outputs (c pre-normalised).
-__device__ void lossGradient(const float *o, float3 wi, float c, float *d, float &loss)
+// Gradient w.r.t. the 41 raw outputs of -c log(a q(wi) + (1 - a) pb), the
+// density of the one-sample MIS proposal the renderer samples from (a = the
+// selection probability, pb = the BSDF lobe's density at wi); c pre-normalised.
+// Lobe gradients are those of -c log q scaled by beta = a q / (a q + (1-a) pb)
+// (or unscaled, wholeTarget: the lobes then fit the whole target).
+__device__ void lossGradient(const float *o, float3 wi, float pb, float c, bool wholeTarget, float *d, float &loss)
 {
     Mixture m;
     decodeOutputs(o, m);
@@ -297,7 +301,13 @@ __device__ void lossGradient(const float *o, float3 wi, float c, float *d, float
         q += m.lobe[k].weight * v[k];
     }
     q = fmaxf(q, 1e-30f);
-    loss = -c * logf(q);
+    const float a = m.select;
+    const float mix = fmaxf(a * q + (1.0f - a) * pb, 1e-30f);
+    loss = -c * logf(mix);
+    const float sg = (a - SELECT_MIN) / SELECT_SPAN;  // sigmoid(logit)
+    d[OUT_SELECT] = -c * (q - pb) / mix * SELECT_SPAN * sg * (1.0f - sg);
+    if (!wholeTarget)
+        c *= a * q / mix;  // else the lobes fit the whole target (-c log q)
 #pragma unroll
     for (int k = 0; k < LOBES; ++k) {
         const Lobe &L = m.lobe[k];
@@ -409,7 +419,7 @@ __global__ void __launch_bounds__(128, 1)
                 d[k] = 0.0f;
             if (c > 0.0f) {
                 float loss;
-                lossGradient(v, f3of4(s.wi), c, d, loss);
+                lossGradient(v, f3of4(s.wi), fmaxf(s.wo.w, 0.0f), c, g.lobeLoss != 0, d, loss);
                 lossAcc += loss;
             }
 #pragma unroll
@@ -664,6 +674,7 @@ GuideGeom guideGeom(const optpt_guide *g)
     r.levels = g->levels;
     r.lo = make_float3(g->lo[0], g->lo[1], g->lo[2]);
     r.invExt = make_float3(g->invExt[0], g->invExt[1], g->invExt[2]);
+    r.lobeLoss = g->lobeLoss;
     return r;
 }
 

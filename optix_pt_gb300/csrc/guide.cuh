@@ -18,6 +18,8 @@ constexpr float RES_MIN = 16.0f, RES_MAX = 256.0f;
 constexpr int WIDTH = 64;             // network width (inputs padded to 64)
 constexpr int LAYERS = 5;             // 64x64 weight matrices: in -> h1 -> h2 -> h3 -> h4 -> out
 constexpr int LOBES = 8;              // vMF lobes; outputs 5k..5k+4 = (mu raw xyz, log kappa, weight logit)
+constexpr int OUT_SELECT = 5 * LOBES; // output 40: logit of the probability of sampling the mixture
+constexpr float SELECT_MIN = 0.02f, SELECT_SPAN = 0.96f;  // that probability = MIN + SPAN * sigmoid(logit)
 constexpr int IN_NORMAL = 2 * LEVELS, IN_WO = IN_NORMAL + 3, IN_ONE = IN_WO + 3;
 constexpr float LOG_KAPPA_MIN = -3.0f, LOG_KAPPA_MAX = 5.5f;
 constexpr size_t HASH_PARAMS = (size_t)LEVELS * TABLE * FEATS;
@@ -57,6 +59,7 @@ struct Lobe {
 };
 struct Mixture {
     Lobe lobe[LOBES];
+    float select;  // probability of sampling the mixture rather than the BSDF
 };
 
 // Normalisation kappa / (2 pi (1 - exp(-2 kappa))), the isotropic 1/(4 pi) as kappa -> 0.
@@ -111,9 +114,11 @@ OPT_D float3 mixtureSample(const Mixture &m, float xi0, float xi1, float xi2)
     return normalize3(w * n + (s * cp) * t + (s * sp) * bt);
 }
 
-// Network outputs o[0..39] -> mixture (softmax weights, exp kappa, unit mu).
+// Network outputs o[0..40] -> mixture (softmax weights, exp kappa, unit mu)
+// and the selection probability.
 OPT_D void decodeOutputs(const float *o, Mixture &m)
 {
+    m.select = SELECT_MIN + SELECT_SPAN / (1.0f + expf(-o[OUT_SELECT]));
     float mx = -1e30f;
 #pragma unroll
     for (int k = 0; k < LOBES; ++k)
@@ -136,13 +141,18 @@ OPT_D void decodeOutputs(const float *o, Mixture &m)
 }
 
 // Packed mixture as stored per ray between the inference and shading kernels:
-// per lobe (mu.xyz, kappa) as 4 halves, then the 8 weights as halves: 80 B.
+// per lobe (mu.xyz, kappa) as 4 halves, the 8 weights, then the selection
+// probability, as halves: 96 B.
 struct alignas(16) Packed {
-    uint4 q[5];
+    uint4 q[6];
 };
 OPT_D void pack(const Mixture &m, Packed &p)
 {
-    __half h[40];
+    __half h[48];
+#pragma unroll
+    for (int k = 40; k < 48; ++k)
+        h[k] = __float2half_rn(0.0f);
+    h[40] = __float2half_rn(m.select);
 #pragma unroll
     for (int k = 0; k < LOBES; ++k) {
         h[4 * k] = __float2half_rn(m.lobe[k].mu.x);
@@ -157,8 +167,9 @@ OPT_D void pack(const Mixture &m, Packed &p)
 // the shading kernel evaluates is exactly the one it samples from.
 OPT_D void unpack(const Packed &p, Mixture &m)
 {
-    __half h[40];
+    __half h[48];
     memcpy(h, &p, sizeof(p));
+    m.select = __half2float(h[40]);
     float sum = 0.0f;
 #pragma unroll
     for (int k = 0; k < LOBES; ++k) {

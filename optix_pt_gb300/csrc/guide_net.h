@@ -21,15 +21,18 @@ struct optpt_guide {
     uint32_t *dStep = nullptr;  // device: Adam step count
     float lr = 1e-2f;
     int numSMs = 0;
+    int lobeLoss = 1;  // 1: lobes fit the whole target (-c log q); 0: what the BSDF leaves (mixture loss)
 };
 
 // Unit-cube mapping and level table as passed to kernels.
 struct GuideGeom {
     guide::Levels levels;
     float3 lo, invExt;
+    int lobeLoss;
 };
 
-// One training sample: (pos.xyz, weight), (n.xyz, -), (wo.xyz, -), (wi.xyz, -).
+// One training sample: (pos.xyz, weight), (n.xyz, -), (wo.xyz, BSDF lobe
+// density at wi), (wi.xyz, -).
 // Weight = target radiance estimate / sampling pdf of wi (the batch is
 // normalised by the sum of weights before the gradient).
 struct GuideSample {

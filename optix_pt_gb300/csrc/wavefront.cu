@@ -261,8 +261,7 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
     float4 *const shEQ[3] = {q.shO[1], q.shD[1], q.shC[1]};
     // guide selection probability: ramps in with training (any value keeps
     // the estimator unbiased; an untrained proposal should be used sparingly)
-    const float alpha =
-        GUIDED ? fp.guide.alphaMax * fminf(1.0f, (float)__ldg(fp.guide.step) / fp.guide.alphaRamp) : 0.0f;
+    const float ramp = GUIDED ? fminf(1.0f, (float)__ldg(fp.guide.step) / fp.guide.alphaRamp) : 0.0f;
 
     for (uint32_t base = warpId * 32u; base < count; base += nWarps * 32u) {
         const uint32_t i = base + (uint32_t)lane;
@@ -514,6 +513,9 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
                                 // the plain estimator, so both integrate over the same set.
                                 guide::Mixture gm;
                                 guide::unpack(reinterpret_cast<const guide::Packed *>(gp.mix)[i], gm);
+                                // selection probability: the network's, phased in with training
+                                const float alpha =
+                                    ramp * fminf(fp.guide.alphaMax, fmaxf(fp.guide.alphaMin, gm.select));
                                 const float uSel = U.next();
                                 if (uSel < alpha)
                                     smp.dir = guide::mixtureSample(gm, xi.x, 1.0f - xi.y, xi.z);
@@ -563,7 +565,7 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
                                         const float3 nIn = dot3(Ng, rayDir) < 0.0f ? Ng : -Ng;
                                         r[0] = mk4(rayOrig + hrec.x * rayDir, pSample);
                                         r[1] = mk4(nIn, __uint_as_float(stamp));
-                                        r[2] = mk4(wo, 0.0f);
+                                        r[2] = mk4(wo, fmaxf(pcLobe, 0.0f));
                                         r[3] = mk4(smp.dir, 0.0f);
                                         r[4] = mk4(fcos, 0.0f);
                                     }

@@ -24,6 +24,7 @@ LEVELS, FEATS, TABLE, WIDTH, LAYERS, LOBES = 16, 2, 1 << 19, 64, 5, 8
 IN_NORMAL, IN_WO, IN_ONE = 32, 35, 38
 LOG_KAPPA_MIN, LOG_KAPPA_MAX = -3.0, 5.5
 WEIGHT_CAP = 16.0
+OUT_SELECT, SELECT_MIN, SELECT_SPAN = 40, 0.02, 0.96
 
 
 def bf16(x):
@@ -110,21 +111,33 @@ def vmf_pdf(mu, kap, wi):
     return norm * np.exp(kap * (t - 1)), t
 
 
+def select_prob(o):
+    """Probability of sampling the mixture instead of the BSDF (output 40)."""
+    return SELECT_MIN + SELECT_SPAN / (1.0 + np.exp(-o[:, OUT_SELECT].astype(np.float64)))
+
+
 def mixture_pdf(o, wi):
     w, mu, kap, *_ = decode(o)
     v, _ = vmf_pdf(mu, kap, wi)
     return (w * v).sum(1)
 
 
-def loss_and_dout(o, wi, c):
-    """Sum over samples of -c log q(wi) and its gradient w.r.t. the outputs."""
+def loss_and_dout(o, wi, c, pb, whole_target=True):
+    """Sum over samples of -c log(a q(wi) + (1 - a) pb) (the one-sample MIS
+    proposal's density) and its gradient w.r.t. the outputs. The selection
+    output always follows that loss; with whole_target the lobe outputs
+    follow -c log q instead (the mixture learns the whole target)."""
     w, mu, kap, raw, ln, lk = decode(o)
     v, t = vmf_pdf(mu, kap, wi)
     q = np.maximum((w * v).sum(1), 1e-30)
-    loss = float((-c * np.log(q)).sum())
+    a = select_prob(o)
+    mix = np.maximum(a * q + (1 - a) * pb, 1e-30)
+    loss = float((-c * np.log(mix)).sum())
     r = w * v / q[:, None]
     d = np.zeros((len(o), WIDTH), np.float64)
-    cc = c[:, None]
+    sg = (a - SELECT_MIN) / SELECT_SPAN
+    d[:, OUT_SELECT] = -c * (q - pb) / mix * SELECT_SPAN * sg * (1 - sg)
+    cc = (c if whole_target else c * a * q / mix)[:, None]
     d[:, 4:5 * LOBES:5] = cc * (w - r)
     dlogc = np.where(kap < 1e-3, (2.0 / 3.0) * kap, 1.0 / kap - 2.0 / np.expm1(2 * kap))
     dk = -cc * r * (dlogc + t - 1)
@@ -150,8 +163,9 @@ def infer(mlp, hash_params, geom, queries):
 
 
 def unpack(packed):
-    """(n, 40) float16 packed mixtures -> weights (n, 8), mu (n, 8, 3), kappa (n, 8)."""
-    h = np.asarray(packed).view(np.float16).reshape(-1, 40).astype(np.float64)
+    """(n, 48) float16 packed mixtures -> weights (n, 8), mu (n, 8, 3), kappa
+    (n, 8); the selection probability is column 40 (`unpack_select`)."""
+    h = np.asarray(packed).view(np.float16).reshape(-1, 48).astype(np.float64)
     mu = h[:, :32].reshape(-1, LOBES, 4)[:, :, :3]
     mu = mu / np.maximum(np.linalg.norm(mu, axis=2, keepdims=True), 1e-6)
     kap = h[:, :32].reshape(-1, LOBES, 4)[:, :, 3]
@@ -160,10 +174,15 @@ def unpack(packed):
     return w, mu, kap
 
 
+def unpack_select(packed):
+    return np.asarray(packed).view(np.float16).reshape(-1, 48)[:, 40].astype(np.float64)
+
+
 def gradients(mlp, hash_params, geom, samples, use_bf16=True):
     """(loss, dMLP (5, 64, 64), dHash (LEVELS * TABLE * 2,)) of a batch.
 
-    samples: (n, 16) float32 = (pos, weight, n, -, wo, -, wi, -)."""
+    samples: (n, 16) float32 = (pos, weight, n, -, wo, pb, wi, -), pb = the
+    BSDF lobe's density at wi."""
     res, dense, lo, inv_ext = geom
     s = np.asarray(samples, np.float32).reshape(-1, 16)
     wgt = s[:, 3].astype(np.float64)
@@ -175,7 +194,7 @@ def gradients(mlp, hash_params, geom, samples, use_bf16=True):
     x0 = encode(hash_params, ent, wts, s[:, 4:7], s[:, 8:11], np.float32 if use_bf16 else np.float64)
     xs, z = forward(mlp, x0, use_bf16)
     W = mlp.reshape(LAYERS, WIDTH, WIDTH)
-    loss, d = loss_and_dout(z, s[:, 12:15].astype(np.float64), c)
+    loss, d = loss_and_dout(z, s[:, 12:15].astype(np.float64), c, np.maximum(s[:, 11], 0).astype(np.float64))
     rnd = bf16 if use_bf16 else (lambda a: a.astype(np.float64))
     dW = np.zeros((LAYERS, WIDTH, WIDTH))
     dz = rnd(d.astype(np.float32)) if use_bf16 else d
@@ -195,22 +214,25 @@ def gradients(mlp, hash_params, geom, samples, use_bf16=True):
     return loss, dW, dH
 
 
-def finite_difference_check(seed=0, n=6, eps=1e-5):
+def finite_difference_check(seed=0, n=6, eps=1e-5, pb_scale=1.0):
     """Max relative error of the analytic FP64 output gradient against
-    central differences of the loss, on random outputs and directions."""
+    central differences of the loss, on random outputs and directions.
+    With pb_scale = 0 the lobe gradients are those of -c log q, the
+    whole-target lobe loss."""
     rng = np.random.default_rng(seed)
     o = rng.normal(size=(n, WIDTH))
     o[:, 3::5] = rng.uniform(-2, 5, size=(n, 13))[:, :13]
     wi = rng.normal(size=(n, 3))
     wi /= np.linalg.norm(wi, axis=1, keepdims=True)
     c = rng.uniform(0.5, 2.0, n)
-    _, d = loss_and_dout(o, wi, c)
+    pb = rng.uniform(0.0, 1.0, n) * pb_scale
+    _, d = loss_and_dout(o, wi, c, pb, whole_target=False)
     worst = 0.0
     for i in range(n):
-        for j in range(5 * LOBES):
+        for j in range(5 * LOBES + 1):
             op, om = o.copy(), o.copy()
             op[i, j] += eps
             om[i, j] -= eps
-            fd = (loss_and_dout(op, wi, c)[0] - loss_and_dout(om, wi, c)[0]) / (2 * eps)
+            fd = (loss_and_dout(op, wi, c, pb, False)[0] - loss_and_dout(om, wi, c, pb, False)[0]) / (2 * eps)
             worst = max(worst, abs(fd - d[i, j]) / max(1e-4, abs(fd) + abs(d[i, j])))
     return worst

@@ -74,6 +74,7 @@ def _samples(rng, n):
     s[:, 3] = rng.exponential(1.0, n)
     s[:, 4:7] = _unit(rng, n)
     s[:, 8:11] = _unit(rng, n)
+    s[:, 11] = rng.uniform(0.0, 1.0, n)   # BSDF lobe density at wi
     s[:, 12:15] = _unit(rng, n)
     s[::17, 3] = 0.0          # zero-weight samples contribute nothing
     s[5, 3] = np.nan          # non-finite weights are ignored
@@ -99,7 +100,7 @@ def test_guide_inference_matches_oracle(cuda_dev):
     n = 1000                                            # 7 full tiles + a ragged one
     q = _queries(rng, n)
     qd = torch.from_numpy(q).to(cuda_dev)
-    out = torch.zeros((n, 40), dtype=torch.float16, device=cuda_dev)
+    out = torch.zeros((n, 48), dtype=torch.float16, device=cuda_dev)
     g.infer(qd.data_ptr(), n, out.data_ptr(), torch.cuda.current_stream())
     torch.cuda.synchronize()
     assert g.status()[0] == 0
@@ -113,6 +114,7 @@ def test_guide_inference_matches_oracle(cuda_dev):
     print("mixture pdf rel err: median %.2e p99 %.2e max %.2e" % (np.median(rel), np.quantile(rel, 0.99), rel.max()))
     assert np.median(rel) < 1e-3 and np.quantile(rel, 0.99) < 5e-3
     assert np.abs(w - wr).max() < 1e-2
+    assert np.abs(go.unpack_select(out.cpu().numpy()) - go.select_prob(o)).max() < 2e-3
     g.close()
 
 
@@ -167,6 +169,7 @@ def test_guide_training_learns_a_directional_target(cuda_dev):
         s[:, 3] = lobe * 4 * np.pi            # target / uniform sampling pdf
         s[:, 4:7] = _unit(rng, n)
         s[:, 8:11] = _unit(rng, n)
+        s[:, 11] = 1 / (4 * np.pi)           # a uniform "BSDF" to mix with
         s[:, 12:15] = wi
         return s
 
@@ -178,7 +181,7 @@ def test_guide_training_learns_a_directional_target(cuda_dev):
         q[:, 8:11] = _unit(rng, n)
         d = target - q[:, 0:3]
         d /= np.linalg.norm(d, axis=1, keepdims=True)
-        out = torch.zeros((n, 40), dtype=torch.float16, device=cuda_dev)
+        out = torch.zeros((n, 48), dtype=torch.float16, device=cuda_dev)
         g.infer(torch.from_numpy(q).to(cuda_dev).data_ptr(), n, out.data_ptr(), torch.cuda.current_stream())
         torch.cuda.synchronize()
         w, mu, kap = go.unpack(out.cpu().numpy())
@@ -193,7 +196,8 @@ def test_guide_training_learns_a_directional_target(cuda_dev):
     torch.cuda.synchronize()
     assert g.status()[0] == 0
     after = score()
-    print("mean log q(target direction): before %.3f after %.3f (uniform %.3f)" % (before, after, np.log(1 / (4 * np.pi))))
+    print("mean log proposal density along the target direction: before %.3f after %.3f (uniform %.3f)" % (
+        before, after, np.log(1 / (4 * np.pi))))
     assert after > before + 2.0
     assert after > np.log(20 / (2 * np.pi)) - 1.5   # near the target lobe's own peak density (log 1.16)
     g.close()

@@ -9,6 +9,7 @@ from oracle import guide_oracle as go
 def test_output_gradient_matches_finite_differences():
     for seed in range(3):
         assert go.finite_difference_check(seed) < 1e-4
+        assert go.finite_difference_check(seed, pb_scale=0.0) < 1e-4   # the whole-target lobe loss
 
 
 def _geom():
