@@ -144,14 +144,18 @@ def _camera_basis(eye, target, up, fov, aspect):
     return list((U * vl * aspect).astype(np.float32)), list((V * vl).astype(np.float32)), list(W.astype(np.float32))
 
 
-def guided_equal_time(stream):
+def guided_equal_time(stream, budget_s=None, reference_spp=None):
     """relMSE (mean over pixels of sum_c (I - R)^2 / (R^2 + 1e-2)) of plain and
     guided renders given the same wall-clock budget, online training included
     in the guided budget; per seed a fresh renderer (and network)."""
     import torch
 
     import optix_pt_gb300 as opt
-    g = GUIDED
+    g = dict(GUIDED)
+    if budget_s:
+        g["budget_s"] = budget_s
+    if reference_spp:
+        g["reference_spp"] = reference_spp
     scene = opt.Scene.procedural(g["scene"])
     w, h = g["width"], g["height"]
 
@@ -196,7 +200,7 @@ def guided_equal_time(stream):
         out[name] = {"relmse": float(np.mean(errs)), "relmse_per_seed": errs, "spp_in_budget": spps,
                      "mrays_per_s": float(np.mean(mrays))}
     out["relmse_ratio_plain_over_guided"] = out["plain"]["relmse"] / out["guided"]["relmse"]
-    out["config"] = dict(GUIDED, reference_seconds=ref_seconds,
+    out["config"] = dict(g, reference_seconds=ref_seconds,
                          protocol="equal wall time per seed, online training inside the guided budget")
     return out
 
@@ -358,7 +362,7 @@ def run_ours(args, rank, world, local_rank):
 
     guided = None
     if world == 1 and not args.no_guided:
-        guided = guided_equal_time(stream)
+        guided = guided_equal_time(stream, args.guided_budget, args.guided_ref_spp)
 
     # CPU baseline: the oracle integrator on this host's cores, bounded band.
     cpu = None
@@ -396,6 +400,9 @@ def main():
     ap.add_argument("--cpu-spp", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain equal-time comparison")
+    ap.add_argument("--guided-only", action="store_true", help="run only the guided-vs-plain comparison")
+    ap.add_argument("--guided-budget", type=float, default=0.0, help="seconds per render (default 2)")
+    ap.add_argument("--guided-ref-spp", type=int, default=0, help="reference spp (default 65536)")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8])
     ap.add_argument("--leaf-size", type=int, default=0)
     ap.add_argument("--block-size", type=int, default=0)
@@ -411,6 +418,12 @@ def main():
     __graft_entry__.build()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.guided_only:
+        import torch
+        torch.cuda.set_device(local_rank)
+        print(json.dumps({"guided_vs_plain_equal_time": guided_equal_time(
+            torch.cuda.Stream(), args.guided_budget, args.guided_ref_spp)}))
         return
     if world > 1:
         import torch.distributed as dist
