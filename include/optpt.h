@@ -285,6 +285,42 @@ int optpt_guide_train_step(optpt_guide *g, const float *samples, const uint32_t 
  * number of samples of the last training step (either may be NULL). */
 int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss, double *lastSamples);
 
+/* ------------------------------------------------------------------ batched multi-view */
+
+/* One camera view of the renderer's scene in a batch: a pinhole camera (the
+ * reference's Camera, src/camera.cpp:19-40), its resolution and samples. */
+typedef struct optpt_view {
+    float eye[3];
+    float target[3];
+    float up[3];
+    float fovYDeg;
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint32_t pad;
+} optpt_view;
+
+/* Renders every view to its spp in shared wavefront passes (the reference
+ * renders one view per launch, src/renderer.cpp:940-1027): the pixels of all
+ * views form one queue, each pass gives every unfinished view's pixels the
+ * same number of samples (at least 1, about 2^21 paths per pass in all), and
+ * the pass is one captured CUDA graph replayed with device-resident sizes.
+ * Each view's image equals what a single-view render of that view would
+ * estimate; its random streams are keyed by the pixel's index in the batch
+ * (view 0 therefore matches a single-view render bit for bit). Guiding, if
+ * on, guides and trains on every view. Accumulators restart at each call. */
+int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numViews, void *stream);
+
+/* Device pointers into the last batch's buffers for one view: FP64 sums and
+ * sums of squares (double4 per pixel, xyz used), the tone-mapped float4
+ * frame buffer, and the samples rendered. Valid until the next batch call
+ * with a different pixel layout. */
+int optpt_batch_view(optpt_renderer *r, uint32_t view, double **sum, double **sumSq, float **frameBuffer,
+                     uint32_t *samples);
+/* Host copies of one view's FP64 sums and sums of squares (4 doubles per
+ * pixel, row-major); either may be NULL. Synchronises `stream`. */
+int optpt_batch_read_view(optpt_renderer *r, uint32_t view, double *sumHost, double *sumSqHost, void *stream);
+
 /* Guided sampling in the renderer (replaces nothing in the reference, whose
  * closest-hit program samples the BSDF only, cu/path_tracer.cu:522-581).
  * mode 0: plain BSDF sampling (bit-identical to a renderer that never had

@@ -294,6 +294,25 @@ class Renderer:
         2: learned guiding, network frozen."""
         check(lib.optpt_set_guiding(self._h, int(mode)))
 
+    def render_batch(self, views, stream=None):
+        """Renders views [(eye, target, up, fovYDeg, width, height, spp), ...]
+        of this scene in shared wavefront passes."""
+        arr = (_ffi.View * len(views))()
+        for i, (eye, target, up, fov, w, h, spp) in enumerate(views):
+            arr[i] = _ffi.View(_ffi.f3(*eye), _ffi.f3(*target), _ffi.f3(*up), fov, w, h, spp, 0)
+        check(lib.optpt_render_batch(self._h, arr, len(views), _stream_handle(stream)))
+        self._batch_shapes = [(v[4], v[5]) for v in views]
+
+    def batch_view(self, v, stream=None):
+        """(sum (h*w, 3) float64, sum of squares, samples) of batch view v."""
+        n = ctypes.c_uint32()
+        check(lib.optpt_batch_view(self._h, v, None, None, None, ctypes.byref(n)))
+        w, h = self._batch_shapes[v]
+        s = np.zeros((h * w, 4), np.float64)
+        q = np.zeros((h * w, 4), np.float64)
+        check(lib.optpt_batch_read_view(self._h, v, s.ctypes.data, q.ctypes.data, _stream_handle(stream)))
+        return s[:, :3], q[:, :3], n.value
+
     def guiding_options(self, **kw):
         """Reads, and with keyword arguments updates, the guiding controls
         (trainSteps, trainStride, maxDepth, alphaMin, alphaMax, alphaRamp,

@@ -117,6 +117,11 @@ class GuidingOptions(ctypes.Structure):
                 ("learningRate", ctypes.c_float), ("lobeLoss", ctypes.c_int32)]
 
 
+class View(ctypes.Structure):
+    _fields_ = [("eye", f3), ("target", f3), ("up", f3), ("fovYDeg", ctypes.c_float), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
 class TraversalCounts(ctypes.Structure):
     _fields_ = [("extensionRays", ctypes.c_uint64), ("extensionNodes", ctypes.c_uint64),
                 ("extensionTris", ctypes.c_uint64), ("shadowRays", ctypes.c_uint64),
@@ -183,6 +188,10 @@ _sigs = {
     "optpt_set_guiding": (ctypes.c_int, [_H, ctypes.c_int]),
     "optpt_get_guide": (ctypes.c_int, [_H, ctypes.POINTER(_P)]),
     "optpt_guiding_batch": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
+    "optpt_render_batch": (ctypes.c_int, [_H, ctypes.POINTER(View), ctypes.c_uint32, _P]),
+    "optpt_batch_read_view": (ctypes.c_int, [_H, ctypes.c_uint32, _P, _P, _P]),
+    "optpt_batch_view": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                        ctypes.POINTER(ctypes.c_uint32)]),
     "optpt_set_guiding_options": (ctypes.c_int, [_H, ctypes.POINTER(GuidingOptions)]),
     "optpt_get_guiding_options": (ctypes.c_int, [_H, ctypes.POINTER(GuidingOptions)]),
 }

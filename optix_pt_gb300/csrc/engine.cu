@@ -97,6 +97,42 @@ struct optpt_renderer {
     int gLobeLoss = 1;
     float sceneLo[3] = {0, 0, 0}, sceneHi[3] = {0, 0, 0};
 
+    // batched multi-view rendering (optpt_render_batch)
+    struct Batch {
+        WaveBufs q{};
+        AccumBufs acc{};
+        BatchView *dViews = nullptr;
+        uint32_t *dPixelList = nullptr, *dDyn = nullptr;
+        uint16_t *dPixelView = nullptr;
+        std::vector<optpt_view> views;
+        std::vector<uint32_t> first, done;
+        uint32_t totalPixels = 0, maxPaths = 0, maxDepth = 0;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int guideMode = -1;
+    } batch;
+
+    void freeBatch()
+    {
+        Batch &b = batch;
+        if (b.exec)
+            cudaGraphExecDestroy(b.exec);
+        if (b.graph)
+            cudaGraphDestroy(b.graph);
+        float4 *bufs[] = {b.q.pathT, b.q.pathL, b.q.rayO[0], b.q.rayO[1], b.q.rayD[0], b.q.rayD[1], b.q.hit,
+                          b.q.shO[0], b.q.shO[1], b.q.shD[0], b.q.shD[1], b.q.shC[0], b.q.shC[1],
+                          b.acc.frameBuffer, b.acc.accumFrameBuffer};
+        for (float4 *p : bufs)
+            cudaFree(p);
+        cudaFree(b.acc.sum);
+        cudaFree(b.acc.sumSq);
+        cudaFree(b.dViews);
+        cudaFree(b.dPixelList);
+        cudaFree(b.dDyn);
+        cudaFree(b.dPixelView);
+        batch = Batch{};
+    }
+
     FrameParams frameParams() const
     {
         FrameParams fp{};
@@ -190,6 +226,7 @@ struct optpt_renderer {
     ~optpt_renderer()
     {
         freeFrame();
+        freeBatch();
         freeGuideBuffers();
         if (guide) {
             guideFree(guide);
@@ -308,8 +345,8 @@ int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
 
 // One pass: sppBatch samples for every pixel.
 // Returns the number of events recorded (profiling), each tagged in `kind`.
-int enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaEvent_t *ev, int *kind,
-                bool count = false)
+int enqueuePassOn(optpt_renderer *r, const FrameParams &fp, const WaveBufs &q, const AccumBufs &acc, cudaStream_t st,
+                  cudaEvent_t *ev, int *kind, bool count = false)
 {
     int e = 0;
     auto mark = [&](int k) {
@@ -319,28 +356,28 @@ int enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaE
             ++e;
         }
     };
-    cudaMemsetAsync(r->q.counters, 0, sizeof(uint32_t) * CNT_TOTAL, st);
+    cudaMemsetAsync(q.counters, 0, sizeof(uint32_t) * CNT_TOTAL, st);
     if (fp.guide.train)
         cudaMemsetAsync(fp.guide.batchCount, 0, sizeof(uint32_t), st);
     mark(0);
-    launchGenerate(r->shape, fp, r->q, st);
+    launchGenerate(r->shape, fp, q, st);
     for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
         mark(1);
-        launchExtend(r->shape, r->scene, fp, r->q, (int)d, st, count);
+        launchExtend(r->shape, r->scene, fp, q, (int)d, st, count);
         if (fp.guide.on && d < fp.maxDepth && d <= fp.guide.maxDepth) {
             mark(5);
-            launchGuideInfer(r->guide, r->scene, fp, r->q, (int)d, st);
+            launchGuideInfer(r->guide, r->scene, fp, q, (int)d, st);
         }
         mark(2);
-        launchShade(r->shape, r->scene, fp, r->q, (int)d, st);
+        launchShade(r->shape, r->scene, fp, q, (int)d, st);
         mark(3);
-        launchShadow(r->shape, r->scene, fp, r->q, (int)d, 0, st, count);
-        launchShadow(r->shape, r->scene, fp, r->q, (int)d, 1, st, count);
+        launchShadow(r->shape, r->scene, fp, q, (int)d, 0, st, count);
+        launchShadow(r->shape, r->scene, fp, q, (int)d, 1, st, count);
     }
     if (fp.guide.train) {
         // online training on this pass's samples (before the pass count advances)
         mark(6);
-        launchGuideGather(fp, r->q, st);
+        launchGuideGather(fp, q, st);
         for (uint32_t k = 0; k < r->gTrainSteps; ++k) {  // minibatches of the pass's samples
             guideGradients(r->guide, reinterpret_cast<const GuideSample *>(fp.guide.batch), fp.guide.batchCount,
                            fp.guide.batchCapacity, st, k, r->gTrainSteps);
@@ -348,18 +385,25 @@ int enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaE
         }
     }
     mark(4);
-    launchAccumulate(r->shape, fp, r->q, r->acc, st);
+    launchAccumulate(r->shape, fp, q, acc, st);
     launchAdvance(fp, r->dState, st);
     mark(7);
     return e;
 }
 
-// Guiding buffers sized for the current frame (paths per pass, max depth).
-int ensureGuideBuffers(optpt_renderer *r)
+int enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaEvent_t *ev, int *kind,
+                bool count = false)
+{
+    return enqueuePassOn(r, fp, r->q, r->acc, st, ev, kind, count);
+}
+
+// Guiding buffers sized for the current frame (paths per pass, max depth),
+// or for `minPaths` paths per pass if that is more (batched rendering).
+int ensureGuideBuffers(optpt_renderer *r, size_t minPaths = 0)
 {
     if (r->guideMode == 0)
         return OPTPT_OK;
-    const size_t paths = (size_t)r->w * r->h * r->sppBatch;
+    const size_t paths = std::max((size_t)r->w * r->h * r->sppBatch, minPaths);
     const size_t slots = ((paths + r->gTrainStride - 1) / r->gTrainStride) * std::max(1u, r->lp.maxDepth);
     if (r->gMix && r->gMixPaths >= paths && r->gRecSlots >= slots)
         return OPTPT_OK;
@@ -380,6 +424,7 @@ int ensureGuideBuffers(optpt_renderer *r)
     r->gMixPaths = paths;
     r->gRecSlots = slots;
     r->graphDirty = true;
+    r->batch.guideMode = -1;  // the batch graph holds the old pointers
     return OPTPT_OK;
 }
 
@@ -688,6 +733,204 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         return rc;
     }
     *out = r;
+    return OPTPT_OK;
+}
+
+int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numViews, void *stream)
+{
+    if (!r || (numViews && !views))
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if (numViews == 0 || numViews > 65535)
+        return fail(OPTPT_ERR_INVALID, "between 1 and 65535 views");
+    uint64_t total = 0;
+    for (uint32_t v = 0; v < numViews; ++v) {
+        const optpt_view &V = views[v];
+        if (V.width == 0 || V.height == 0 || V.spp == 0 || !(V.fovYDeg > 0.0f && V.fovYDeg < 180.0f))
+            return fail(OPTPT_ERR_INVALID, "view " + std::to_string(v) + ": width, height, spp > 0, fovYDeg in (0, 180)");
+        total += (uint64_t)V.width * V.height;
+    }
+    if (total > (1u << 30))
+        return fail(OPTPT_ERR_INVALID, "more than 2^30 pixels in one batch");
+    cudaStream_t st = (cudaStream_t)stream;
+    auto &B = r->batch;
+    if (r->shape.block == 0) {
+        const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 128;
+        r->shape.block = blk;
+        r->shape.gridGenerate = occupancyGrid(0, blk);
+        const bool wide = r->bvh.nodes8 != nullptr;
+        r->shape.gridExtend = occupancyGrid(wide ? 1 : 11, blk);
+        r->shape.gridShade = occupancyGrid(2, blk);
+        r->shape.gridShadow = occupancyGrid(wide ? 3 : 13, blk);
+        r->shape.gridAccum = occupancyGrid(4, blk);
+    }
+    // (Re)allocate when the pixel layout changes; paths per pass: at least one
+    // sample for every pixel, and about 2^21 paths when fewer pixels are active.
+    bool layout = B.views.size() != numViews || B.maxDepth != r->lp.maxDepth;
+    for (uint32_t v = 0; !layout && v < numViews; ++v)
+        layout = B.views[v].width != views[v].width || B.views[v].height != views[v].height;
+    if (layout) {
+        r->freeBatch();
+        B.totalPixels = (uint32_t)total;
+        B.maxPaths = std::max<uint32_t>(B.totalPixels, 1u << 21);
+        B.maxDepth = r->lp.maxDepth;
+        const size_t P = B.maxPaths, N = B.totalPixels;
+        cudaError_t e = cudaSuccess;
+        auto al = [&](void **p, size_t bytes) {
+            if (e == cudaSuccess)
+                e = cudaMalloc(p, bytes ? bytes : 16);
+        };
+        float4 **bufs[] = {&B.q.pathT, &B.q.pathL, &B.q.rayO[0], &B.q.rayO[1], &B.q.rayD[0], &B.q.rayD[1], &B.q.hit,
+                           &B.q.shO[0], &B.q.shO[1], &B.q.shD[0], &B.q.shD[1], &B.q.shC[0], &B.q.shC[1]};
+        for (float4 **b : bufs)
+            al((void **)b, sizeof(float4) * P);
+        al((void **)&B.acc.sum, sizeof(Acc4) * N);
+        al((void **)&B.acc.sumSq, sizeof(Acc4) * N);
+        al((void **)&B.acc.frameBuffer, sizeof(float4) * N);
+        al((void **)&B.acc.accumFrameBuffer, sizeof(float4) * N);
+        al((void **)&B.dViews, sizeof(BatchView) * numViews);
+        al((void **)&B.dPixelList, sizeof(uint32_t) * N);
+        al((void **)&B.dPixelView, sizeof(uint16_t) * N);
+        al((void **)&B.dDyn, sizeof(uint32_t) * 2);
+        if (e != cudaSuccess) {
+            r->freeBatch();
+            return fail(OPTPT_ERR_NOMEM, std::string("batch buffers: ") + cudaGetErrorString(e));
+        }
+        B.views.assign(views, views + numViews);
+        B.first.resize(numViews);
+        std::vector<uint16_t> pv(N);
+        uint32_t at = 0;
+        for (uint32_t v = 0; v < numViews; ++v) {
+            B.first[v] = at;
+            const uint32_t n = views[v].width * views[v].height;
+            std::fill(pv.begin() + at, pv.begin() + at + n, (uint16_t)v);
+            at += n;
+        }
+        CUDA_OR_RETURN(cudaMemcpy(B.dPixelView, pv.data(), sizeof(uint16_t) * N, cudaMemcpyHostToDevice), "batch");
+    }
+    B.views.assign(views, views + numViews);
+    B.q.counters = r->q.counters;
+    B.q.totals = r->q.totals;
+    int rc = ensureGuideBuffers(r, B.maxPaths);
+    if (rc)
+        return rc;
+    CUDA_OR_RETURN(cudaMemsetAsync(B.acc.sum, 0, sizeof(Acc4) * B.totalPixels, st), "batch");
+    CUDA_OR_RETURN(cudaMemsetAsync(B.acc.sumSq, 0, sizeof(Acc4) * B.totalPixels, st), "batch");
+    B.done.assign(numViews, 0u);
+    const FrameConst fc = r->frameConst();
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+
+    FrameParams fp = r->frameParams();
+    fp.w = fp.h = fp.npix = fp.sppBatch = 0;
+    fp.numPaths = B.maxPaths;
+    fp.batch = BatchPass{B.dViews, B.dPixelList, B.dPixelView, B.dDyn, 1u};
+    if (fp.guide.on) {  // the guiding buffers now hold the batch's paths
+        fp.guide.mix = r->gMix;
+        fp.guide.rec = r->gRec;
+    }
+    // one captured pass; every replay reads its sizes from the device
+    if (!B.exec || B.guideMode != r->guideMode || r->graphDirty) {
+        if (B.exec)
+            cudaGraphExecDestroy(B.exec);
+        if (B.graph)
+            cudaGraphDestroy(B.graph);
+        B.exec = nullptr;
+        B.graph = nullptr;
+        cudaStream_t cs = st ? st : r->ownStream;
+        CUDA_OR_RETURN(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "batch capture");
+        enqueuePassOn(r, fp, B.q, B.acc, cs, nullptr, nullptr);
+        cudaError_t e = cudaStreamEndCapture(cs, &B.graph);
+        if (e != cudaSuccess)
+            return cudaFail(e, "batch capture");
+        CUDA_OR_RETURN(cudaGraphInstantiate(&B.exec, B.graph, 0), "batch instantiate");
+        B.guideMode = r->guideMode;
+    }
+    std::vector<BatchView> hv(numViews);
+    std::vector<uint32_t> list;
+    std::vector<char> wasActive(numViews, 0);
+    for (;;) {
+        uint32_t active = 0, minLeft = UINT32_MAX;
+        bool changed = false;
+        for (uint32_t v = 0; v < numViews; ++v) {
+            const bool a = B.done[v] < views[v].spp;
+            changed |= (a != (bool)wasActive[v]);
+            wasActive[v] = a;
+            if (a) {
+                active += views[v].width * views[v].height;
+                minLeft = std::min(minLeft, views[v].spp - B.done[v]);
+            }
+        }
+        if (active == 0)
+            break;
+        if (changed) {
+            list.clear();
+            for (uint32_t v = 0; v < numViews; ++v)
+                if (wasActive[v])
+                    for (uint32_t k = 0; k < views[v].width * views[v].height; ++k)
+                        list.push_back(B.first[v] + k);
+            CUDA_OR_RETURN(cudaMemcpyAsync(B.dPixelList, list.data(), sizeof(uint32_t) * list.size(),
+                                           cudaMemcpyHostToDevice, st),
+                           "batch list");
+        }
+        const uint32_t per = std::max(1u, std::min(minLeft, B.maxPaths / active));
+        for (uint32_t v = 0; v < numViews; ++v) {
+            const optpt_view &V = views[v];
+            float U[3], Vv[3], W[3];
+            cameraBasis(V.eye, V.target, V.up, V.fovYDeg, (float)V.width / (float)V.height, U, Vv, W);
+            auto bits = [](uint32_t u) {
+                float f;
+                memcpy(&f, &u, 4);
+                return f;
+            };
+            hv[v].eye = make_float4(V.eye[0], V.eye[1], V.eye[2], bits(V.width));
+            hv[v].U = make_float4(U[0], U[1], U[2], bits(V.height));
+            hv[v].V = make_float4(Vv[0], Vv[1], Vv[2], bits(B.first[v]));
+            hv[v].W = make_float4(W[0], W[1], W[2], bits(B.done[v]));
+        }
+        const uint32_t dyn[2] = {active, per};
+        CUDA_OR_RETURN(cudaMemcpyAsync(B.dViews, hv.data(), sizeof(BatchView) * numViews, cudaMemcpyHostToDevice, st),
+                       "batch views");
+        CUDA_OR_RETURN(cudaMemcpyAsync(B.dDyn, dyn, sizeof(dyn), cudaMemcpyHostToDevice, st), "batch sizes");
+        CUDA_OR_RETURN(cudaGraphLaunch(B.exec, st), "batch launch");
+        for (uint32_t v = 0; v < numViews; ++v)
+            if (wasActive[v])
+                B.done[v] += per;
+    }
+    CUDA_OR_RETURN(cudaGetLastError(), "batch");
+    return OPTPT_OK;
+}
+
+int optpt_batch_view(optpt_renderer *r, uint32_t view, double **sum, double **sumSq, float **frameBuffer,
+                     uint32_t *samples)
+{
+    if (!r)
+        return fail(OPTPT_ERR_INVALID, "NULL renderer");
+    if (view >= r->batch.views.size())
+        return fail(OPTPT_ERR_INVALID, "no such view in the last batch");
+    const uint32_t f = r->batch.first[view];
+    if (sum)
+        *sum = reinterpret_cast<double *>(r->batch.acc.sum + f);
+    if (sumSq)
+        *sumSq = reinterpret_cast<double *>(r->batch.acc.sumSq + f);
+    if (frameBuffer)
+        *frameBuffer = reinterpret_cast<float *>(r->batch.acc.frameBuffer + f);
+    if (samples)
+        *samples = r->batch.done.empty() ? 0u : r->batch.done[view];
+    return OPTPT_OK;
+}
+
+int optpt_batch_read_view(optpt_renderer *r, uint32_t view, double *sumHost, double *sumSqHost, void *stream)
+{
+    double *s = nullptr, *q = nullptr;
+    int rc = optpt_batch_view(r, view, &s, &q, nullptr, nullptr);
+    if (rc)
+        return rc;
+    const size_t n = (size_t)r->batch.views[view].width * r->batch.views[view].height;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (sumHost)
+        CUDA_OR_RETURN(cudaMemcpyAsync(sumHost, s, sizeof(Acc4) * n, cudaMemcpyDeviceToHost, st), "read view");
+    if (sumSqHost)
+        CUDA_OR_RETURN(cudaMemcpyAsync(sumSqHost, q, sizeof(Acc4) * n, cudaMemcpyDeviceToHost, st), "read view");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "read view");
     return OPTPT_OK;
 }
 

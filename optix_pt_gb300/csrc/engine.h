@@ -95,6 +95,24 @@ __host__ __device__ inline uint32_t guideTrainOffset(uint32_t group, uint32_t st
     return h % stride;
 }
 
+// Batched multi-view rendering: the pixels of all views are concatenated
+// (view v owns global pixels first .. first + width * height - 1). A pass
+// renders `dyn[1]` samples for each of the `dyn[0]` active global pixels in
+// `pixelList`; path p is sample p / dyn[0] of pixel pixelList[p % dyn[0]].
+struct BatchView {
+    float4 eye;  // xyz; w = width (uint bits)
+    float4 U;    // xyz; w = height (uint bits)
+    float4 V;    // xyz; w = first global pixel (uint bits)
+    float4 W;    // xyz; w = samples accumulated before this pass (uint bits)
+};
+struct BatchPass {
+    const BatchView *views;
+    const uint32_t *pixelList;  // active global pixels of this pass
+    const uint16_t *pixelView;  // view of every global pixel
+    const uint32_t *dyn;        // [0] active pixels, [1] samples per active pixel
+    uint32_t on;
+};
+
 // Launch-shape parameters baked into a captured pass.
 struct FrameParams {
     uint32_t w, h, npix, sppBatch, numPaths;
@@ -102,7 +120,28 @@ struct FrameParams {
     const uint32_t *state;   // device: [0] = samples accumulated before this pass, [1] = passes run
     const FrameConst *fc;    // device
     GuidePass guide;
+    BatchPass batch;
 };
+
+// Global pixel (the RNG's pixel key) and sample index of a path.
+__device__ __forceinline__ void pathPixelSample(const FrameParams &fp, uint32_t path, uint32_t &pixel,
+                                                uint32_t &sample)
+{
+    if (fp.batch.on) {
+        const uint32_t n = __ldg(fp.batch.dyn);
+        pixel = __ldg(fp.batch.pixelList + path % n);
+        const uint32_t v = __ldg(fp.batch.pixelView + pixel);
+        sample = __float_as_uint(__ldg(&fp.batch.views[v].W).w) + path / n;
+    } else {
+        pixel = path % fp.npix;
+        sample = __ldg(fp.state) + path / fp.npix;
+    }
+}
+// Paths of this pass (device-resident in batch mode).
+__device__ __forceinline__ uint32_t passPaths(const FrameParams &fp)
+{
+    return fp.batch.on ? __ldg(fp.batch.dyn) * __ldg(fp.batch.dyn + 1) : fp.numPaths;
+}
 
 // Device counters: per-depth queue lengths. Depth d uses index d.
 #define CNT_EXT 0

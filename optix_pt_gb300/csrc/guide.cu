@@ -553,7 +553,8 @@ __global__ void kGuideGather(FrameParams fp, WaveBufs q)
 {
     const GuidePass gp = fp.guide;
     const uint32_t stamp = __ldg(fp.state + 1) + 1u;
-    const uint32_t numTrain = (fp.numPaths + gp.trainStride - 1u) / gp.trainStride;
+    const uint32_t numPaths = passPaths(fp);
+    const uint32_t numTrain = (numPaths + gp.trainStride - 1u) / gp.trainStride;
     const uint32_t total = numTrain * fp.maxDepth;
     GuideSample *batch = reinterpret_cast<GuideSample *>(gp.batch);
     for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
@@ -563,7 +564,7 @@ __global__ void kGuideGather(FrameParams fp, WaveBufs q)
             continue;
         const uint32_t group = idx / fp.maxDepth;
         const uint32_t path = group * gp.trainStride + guideTrainOffset(group, stamp, gp.trainStride);
-        if (path >= fp.numPaths)
+        if (path >= numPaths)
             continue;
         const float3 Lf = f3of4(q.pathL[path]), Ls = f3of4(r5), Ta = f3of4(r[6]), fc = f3of4(r[4]);
         const float3 dL = Lf - Ls;

@@ -116,15 +116,35 @@ __global__ void __launch_bounds__(256) kGenerate(FrameParams fp, WaveBufs q)
     const uint32_t sampleBase = __ldg(fp.state);
     const float4 e4 = __ldg(&fp.fc->eye), u4 = __ldg(&fp.fc->U), v4 = __ldg(&fp.fc->V), w4 = __ldg(&fp.fc->W);
     const uint32_t seed = __float_as_uint(e4.w);
-    const float3 eye = f3of4(e4), camU = f3of4(u4), camV = f3of4(v4), camW = f3of4(w4);
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < fp.numPaths; p += stride) {
-        const uint32_t pixel = p % fp.npix, b = p / fp.npix;
-        const uint32_t x = pixel % fp.w, y = pixel / fp.w;
-        Pcg32 rng = pathRng(seed, pixel, sampleBase + b, 0u);
+    float3 eye = f3of4(e4), camU = f3of4(u4), camV = f3of4(v4), camW = f3of4(w4);
+    const uint32_t numPaths = passPaths(fp);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < numPaths; p += stride) {
+        uint32_t pixel, sample, x, y, w = fp.w, h = fp.h;
+        if (fp.batch.on) {
+            // the path's view: its camera and resolution (batched multi-view)
+            pathPixelSample(fp, p, pixel, sample);
+            const BatchView &V = fp.batch.views[__ldg(fp.batch.pixelView + pixel)];
+            const float4 ve = __ldg(&V.eye), vu = __ldg(&V.U), vv = __ldg(&V.V), vw = __ldg(&V.W);
+            eye = f3of4(ve);
+            camU = f3of4(vu);
+            camV = f3of4(vv);
+            camW = f3of4(vw);
+            w = __float_as_uint(ve.w);
+            h = __float_as_uint(vu.w);
+            const uint32_t local = pixel - __float_as_uint(vv.w);
+            x = local % w;
+            y = local / w;
+        } else {
+            pixel = p % fp.npix;
+            sample = sampleBase + p / fp.npix;
+            x = pixel % fp.w;
+            y = pixel / fp.w;
+        }
+        Pcg32 rng = pathRng(seed, pixel, sample, 0u);
         const float jx = rng.uniform(), jy = rng.uniform();
         const float fx = (float)x + jx, fy = (float)y + jy;
-        const float ndcx = (fx / (float)fp.w) * 2.0f + -1.0f;
-        const float ndcy = (fy / (float)fp.h) * -2.0f + 1.0f;
+        const float ndcx = (fx / (float)w) * 2.0f + -1.0f;
+        const float ndcy = (fy / (float)h) * -2.0f + 1.0f;
         const float3 dir = normalize3(ndcx * camU + ndcy * camV + camW);
         q.rayO[1][p] = mk4(eye, __int_as_float((int)p));
         q.rayD[1][p] = mk4(dir, 0.0f);
@@ -132,7 +152,7 @@ __global__ void __launch_bounds__(256) kGenerate(FrameParams fp, WaveBufs q)
         q.pathL[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
-        q.counters[CNT_EXT + 1] = fp.numPaths;
+        q.counters[CNT_EXT + 1] = numPaths;
 }
 
 // ------------------------------------------------------------------ extend
@@ -163,7 +183,9 @@ __global__ void __launch_bounds__(256, OPTPT_TRAV_MINB) kExtend(DevScene s, Fram
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
         const float4 ro = q.rayO[cur][i], rd = q.rayD[cur][i];
         const uint32_t path = (uint32_t)__float_as_int(ro.w);
-        const AlphaTest at = makeAlpha(s, seed, path % fp.npix, sampleBase + path / fp.npix, (uint32_t)depth, -1.0f);
+        uint32_t pixel, sample;
+        pathPixelSample(fp, path, pixel, sample);
+        const AlphaTest at = makeAlpha(s, seed, pixel, sample, (uint32_t)depth, -1.0f);
         HitRec h;
         const bool hit = traceScene<false, WIDE>(s, f3of4(ro), f3of4(rd), 0.0f, 1e16f, h, at, ctr);
         q.hit[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.leaf))
@@ -294,7 +316,8 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
             if (leaf < 0) {
                 L = L + bg * T;
             } else {
-                const uint32_t pixel = path % fp.npix, sample = sampleBase + path / fp.npix;
+                uint32_t pixel, sample;
+                pathPixelSample(fp, path, pixel, sample);
                 Pcg32 rng = pathRng(seed, pixel, sample, (uint32_t)depth);
                 PcgSource U{&rng};
                 const float4 t0 = __ldg(&s.triV[3 * leaf]), t1 = __ldg(&s.triV[3 * leaf + 1]),
@@ -602,7 +625,9 @@ __global__ void __launch_bounds__(256, OPTPT_TRAV_MINB)
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
         const float4 o = q.shO[which][j], d = q.shD[which][j], c = q.shC[which][j];
         const uint32_t path = (uint32_t)__float_as_int(o.w);
-        const AlphaTest at = makeAlpha(s, seed, path % fp.npix, sampleBase + path / fp.npix, (uint32_t)depth, c.w);
+        uint32_t pixel, sample;
+        pathPixelSample(fp, path, pixel, sample);
+        const AlphaTest at = makeAlpha(s, seed, pixel, sample, (uint32_t)depth, c.w);
         HitRec h;
         const bool occluded =
             traceScene<true, WIDE>(s, f3of4(o), f3of4(d), OPT_SCENE_EPSILON, d.w, h, at, ctr);
@@ -630,11 +655,17 @@ __global__ void __launch_bounds__(256) kAccumulate(FrameParams fp, WaveBufs q, A
     const int toneFlags = __float_as_int(__ldg(&fp.fc->V).w);
     const float gammaTerm = __ldg(&fp.fc->W).w;
     uint32_t nanLocal = 0;
-    for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < fp.npix; px += stride) {
+    const uint32_t active = fp.batch.on ? __ldg(fp.batch.dyn) : fp.npix;
+    const uint32_t perPixel = fp.batch.on ? __ldg(fp.batch.dyn + 1) : fp.sppBatch;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < active; i += stride) {
+        uint32_t px = i, n = samplesBefore;
+        if (fp.batch.on) {  // active pixel i of the batch: its global pixel and view's sample count
+            px = __ldg(fp.batch.pixelList + i);
+            n = __float_as_uint(__ldg(&fp.batch.views[__ldg(fp.batch.pixelView + px)].W).w);
+        }
         Acc4 S = a.sum[px], Q = a.sumSq[px];
-        uint32_t n = samplesBefore;
-        for (uint32_t b = 0; b < fp.sppBatch; ++b) {
-            const float4 Lf = q.pathL[b * fp.npix + px];
+        for (uint32_t b = 0; b < perPixel; ++b) {
+            const float4 Lf = q.pathL[b * active + i];
             double lx, ly, lz;
             if (isnan(Lf.x) || isnan(Lf.y) || isnan(Lf.z)) {
                 ++nanLocal;
@@ -685,7 +716,7 @@ __global__ void __launch_bounds__(256) kAccumulate(FrameParams fp, WaveBufs q, A
         }
         q.totals[0] += ext;
         q.totals[1] += sh;
-        q.totals[2] += fp.numPaths;
+        q.totals[2] += (unsigned long long)active * perPixel;
     }
 }
 
