@@ -205,6 +205,86 @@ def guided_equal_time(stream, budget_s=None, reference_spp=None):
     return out
 
 
+BATCH = {"workload": "batched multi-view: 96 views (48 of the terrain, 48 of the material sweep), sides "
+                     "log-uniform 128..1024, spp U{16..256}, depth 12, guiding on; one batch per scene, each "
+                     "autotuned (leaf size, block size, compaction)", "views_per_scene": 48, "seed": 5}
+
+
+def _batch_views(scene, n, rng):
+    a = scene.arrays()
+    eye0, tgt0 = np.array(a["camEye"]), np.array(a["camTarget"])
+    span = np.linalg.norm(tgt0 - eye0)
+    views = []
+    for _ in range(n):
+        side = 128.0 * 8.0 ** rng.uniform()                 # log-uniform 128 .. 1024
+        aspect = rng.uniform(0.6, 1.8)
+        w = int(max(16, round(side * np.sqrt(aspect))))
+        h = int(max(16, round(side / np.sqrt(aspect))))
+        eye = eye0 + rng.normal(scale=0.15 * span, size=3)
+        tgt = tgt0 + rng.normal(scale=0.1 * span, size=3)
+        views.append((list(eye), list(tgt), [0.0, 1.0, 0.0], float(a["camFovYDeg"]), w, h, int(rng.integers(16, 257))))
+    return views
+
+
+def run_batch(args):
+    """Batched multi-view workload: aggregate throughput of one batch per scene
+    (autotuned), and relMSE of a few views against 16x-spp single-view renders."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    stream = torch.cuda.Stream()
+    rng = np.random.default_rng(BATCH["seed"])
+    per_scene, rays_all, samples_all, seconds_all = [], 0, 0, 0.0
+    for name in ("terrain", "spheres"):
+        scene = opt.Scene.procedural(name)
+        best, trials = opt.autotune(scene, 320, 180, 16)
+        r = opt.Renderer(scene, leaf_size=best["leafSize"], block_size=best["blockSize"],
+                         compaction=best["compaction"])
+        r.set_max_depth(12)
+        r.set_guiding(1)
+        views = _batch_views(scene, BATCH["views_per_scene"], rng)
+        r.render_batch(views[:2], stream)            # warm-up: graph capture, network allocation
+        torch.cuda.synchronize()
+        st0 = r.stats()
+        t0 = time.perf_counter()
+        r.render_batch(views, stream)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        st1 = r.stats()
+        rays = (st1["extensionRays"] - st0["extensionRays"]) + (st1["shadowRays"] - st0["shadowRays"])
+        samples = st1["pathSamples"] - st0["pathSamples"]
+        # per-view relMSE: the two smallest views against plain 16x-spp renders
+        small = sorted(range(len(views)), key=lambda k: views[k][4] * views[k][5])[:2]
+        rel = {}
+        for k in small:
+            eye, tgt, up, fov, w, h, spp = views[k]
+            s, _, n = r.batch_view(k)
+            ref = opt.Renderer(scene)
+            ref.setupOutputBuffer(w, h)
+            ref.setupCamera(eye, tgt, up, fov)
+            ref.set_max_depth(12)
+            ref.render(16 * spp, stream)
+            torch.cuda.synchronize()
+            rs, _, rn = ref.accum()
+            R = rs.reshape(-1, 3) / rn
+            I = s / n
+            rel["view%d_%dx%d_%dspp" % (k, w, h, spp)] = float(np.mean(((I - R) ** 2 / (R ** 2 + 1e-2)).sum(1)))
+            ref.close()
+        per_scene.append({"scene": name, "views": len(views), "pixels": int(sum(v[4] * v[5] for v in views)),
+                          "samples": int(samples), "seconds": dt, "mrays_per_s": rays / dt / 1e6,
+                          "msamples_per_s": samples / dt / 1e6, "autotuned": best, "relmse_vs_16x_spp": rel,
+                          "guide_status": r.guide().status()})
+        rays_all += rays
+        samples_all += samples
+        seconds_all += dt
+        r.close()
+    line = {"metric": "Mrays/s, batched multi-view (aggregate)", "value": rays_all / seconds_all / 1e6,
+            "unit": "Mrays/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded procedural scenes and views)", "config": dict(BATCH),
+            "msamples_per_s": samples_all / seconds_all / 1e6, "per_scene": per_scene}
+    print(json.dumps(line))
+
+
 def run_reference(args, rank, world):
     """The reference arm: the oracle integrator on the host cores."""
     if rank != 0:
@@ -396,7 +476,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sweep", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="sweep", choices=sorted(WORKLOADS) + ["batch"])
     ap.add_argument("--cpu-spp", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain equal-time comparison")
@@ -408,9 +488,10 @@ def main():
     ap.add_argument("--block-size", type=int, default=0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-    WORKLOAD.clear()
-    WORKLOAD.update(WORKLOADS[args.workload])
-    args.cpu_spp = args.cpu_spp or CPU_SPP[args.workload]
+    if args.workload in WORKLOADS:
+        WORKLOAD.clear()
+        WORKLOAD.update(WORKLOADS[args.workload])
+        args.cpu_spp = args.cpu_spp or CPU_SPP[args.workload]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -418,6 +499,9 @@ def main():
     __graft_entry__.build()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "batch":
+        run_batch(args)
         return
     if args.guided_only:
         import torch

@@ -110,6 +110,8 @@ typedef struct optpt_options {
                           * (0 = 1), 1..8 for the binary one (0 = 4)                */
     uint32_t useGraph;   /* capture the bounce loop in a CUDA graph (default 1)      */
     uint32_t bvhWidth;   /* 8: compressed 8-wide BVH (default), 2: the binary LBVH   */
+    uint32_t compaction; /* queue appends: 0 = auto (one atomic per warp), 32 = per
+                          * warp, 1 = per block (one atomic per block and queue)   */
 } optpt_options;
 
 /* Uploads the scene and builds the BVH on the GPU. Replaces the reference's
@@ -284,6 +286,30 @@ int optpt_guide_train_step(optpt_guide *g, const float *samples, const uint32_t 
 /* *status = 1 if a tensor-core completion wait expired; the loss and the
  * number of samples of the last training step (either may be NULL). */
 int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss, double *lastSamples);
+
+/* ------------------------------------------------------------------ autotuner */
+
+/* Picks the BVH8 leaf size (1, 2, 3), the wavefront block size (64, 128, 256)
+ * and the shading-queue compaction (per warp, per block) that render the
+ * scene fastest (pixel-samples per second) at width x height with `spp`
+ * samples timed after `warmupSpp` untimed ones (0 = 2), guiding mode
+ * `guiding` (0 plain; see optpt_set_guiding). The reference has no
+ * counterpart: OptiX makes these choices internally. One renderer per
+ * candidate; `trials` (optional) receives every measurement. */
+typedef struct optpt_autotune_request {
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint32_t warmupSpp;
+    uint32_t guiding;
+} optpt_autotune_request;
+typedef struct optpt_autotune_trial {
+    optpt_options options;
+    double samplesPerS;
+    double mraysPerS;
+} optpt_autotune_trial;
+int optpt_autotune(const optpt_scene *scene, const optpt_autotune_request *req, optpt_options *best,
+                   optpt_autotune_trial *trials, uint32_t maxTrials, uint32_t *numTrials);
 
 /* ------------------------------------------------------------------ batched multi-view */
 

@@ -94,9 +94,9 @@ SceneDesc = Scene.from_config  # the reference constructs SceneDesc from the sce
 class Renderer:
     """The reference's Renderer (include/renderer.h:19-206) on the GB300 engine."""
 
-    def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True, bvh_width=8):
+    def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True, bvh_width=8, compaction=0):
         self.scene = scene
-        opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0, bvh_width)
+        opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0, bvh_width, compaction)
         h = ctypes.c_void_p()
         check(lib.optpt_create(ctypes.byref(scene.struct), ctypes.byref(opt), ctypes.byref(h)))
         self._h = h
@@ -425,3 +425,17 @@ class Guide:
         n = ctypes.c_double()
         check(lib.optpt_guide_status(self._h, ctypes.byref(st), ctypes.byref(loss), ctypes.byref(n)))
         return st.value, loss.value, n.value
+
+
+def autotune(scene, width, height, spp, warmup_spp=2, guiding=0):
+    """Times every (leaf size, block size, compaction) candidate on `scene`;
+    returns (best options as a dict, [trial dicts])."""
+    req = _ffi.AutotuneRequest(width, height, spp, warmup_spp, guiding)
+    best = _ffi.Options()
+    trials = (_ffi.AutotuneTrial * 64)()
+    n = ctypes.c_uint32()
+    check(lib.optpt_autotune(ctypes.byref(scene.struct), ctypes.byref(req), ctypes.byref(best), trials, 64,
+                             ctypes.byref(n)))
+    opts = lambda o: {k: getattr(o, k) for k, _ in o._fields_}
+    return opts(best), [dict(opts(t.options), samples_per_s=t.samplesPerS, mrays_per_s=t.mraysPerS)
+                        for t in trials[:n.value]]

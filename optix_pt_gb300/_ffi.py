@@ -96,7 +96,7 @@ class SceneStruct(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32), ("leafSize", ctypes.c_uint32),
-                ("useGraph", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32)]
+                ("useGraph", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32), ("compaction", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -115,6 +115,15 @@ class GuidingOptions(ctypes.Structure):
     _fields_ = [("trainSteps", ctypes.c_uint32), ("trainStride", ctypes.c_uint32), ("maxDepth", ctypes.c_uint32),
                 ("alphaMin", ctypes.c_float), ("alphaMax", ctypes.c_float), ("alphaRamp", ctypes.c_float),
                 ("learningRate", ctypes.c_float), ("lobeLoss", ctypes.c_int32)]
+
+
+class AutotuneRequest(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32),
+                ("warmupSpp", ctypes.c_uint32), ("guiding", ctypes.c_uint32)]
+
+
+class AutotuneTrial(ctypes.Structure):
+    _fields_ = [("options", Options), ("samplesPerS", ctypes.c_double), ("mraysPerS", ctypes.c_double)]
 
 
 class View(ctypes.Structure):
@@ -189,6 +198,9 @@ _sigs = {
     "optpt_get_guide": (ctypes.c_int, [_H, ctypes.POINTER(_P)]),
     "optpt_guiding_batch": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
     "optpt_render_batch": (ctypes.c_int, [_H, ctypes.POINTER(View), ctypes.c_uint32, _P]),
+    "optpt_autotune": (ctypes.c_int, [ctypes.POINTER(SceneStruct), ctypes.POINTER(AutotuneRequest),
+                                      ctypes.POINTER(Options), ctypes.POINTER(AutotuneTrial), ctypes.c_uint32,
+                                      ctypes.POINTER(ctypes.c_uint32)]),
     "optpt_batch_read_view": (ctypes.c_int, [_H, ctypes.c_uint32, _P, _P, _P]),
     "optpt_batch_view": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
                                         ctypes.POINTER(ctypes.c_uint32)]),

@@ -333,6 +333,7 @@ int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
     r->hostFbValid = false;
     const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 128;
     r->shape.block = blk;
+    r->shape.compaction = r->opt.compaction == 1 ? 1 : 0;
     r->shape.gridGenerate = occupancyGrid(0, blk);
     const bool wide = r->bvh.nodes8 != nullptr;
     r->shape.gridExtend = occupancyGrid(wide ? 1 : 11, blk);
@@ -399,12 +400,13 @@ int enqueuePass(optpt_renderer *r, const FrameParams &fp, cudaStream_t st, cudaE
 
 // Guiding buffers sized for the current frame (paths per pass, max depth),
 // or for `minPaths` paths per pass if that is more (batched rendering).
-int ensureGuideBuffers(optpt_renderer *r, size_t minPaths = 0)
+int ensureGuideBuffers(optpt_renderer *r, size_t minPaths = 0, uint32_t stride = 0)
 {
     if (r->guideMode == 0)
         return OPTPT_OK;
     const size_t paths = std::max((size_t)r->w * r->h * r->sppBatch, minPaths);
-    const size_t slots = ((paths + r->gTrainStride - 1) / r->gTrainStride) * std::max(1u, r->lp.maxDepth);
+    stride = std::max(stride, r->gTrainStride);
+    const size_t slots = ((paths + stride - 1) / stride) * std::max(1u, r->lp.maxDepth);
     if (r->gMix && r->gMixPaths >= paths && r->gRecSlots >= slots)
         return OPTPT_OK;
     r->freeGuideBuffers();
@@ -582,6 +584,14 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         delete r;
         return fail(OPTPT_ERR_INVALID, "bvhWidth must be 2 or 8");
     }
+    if (r->opt.compaction != 0 && r->opt.compaction != 1 && r->opt.compaction != 32) {
+        delete r;
+        return fail(OPTPT_ERR_INVALID, "compaction must be 0 (auto), 1 (per block) or 32 (per warp)");
+    }
+    if (r->opt.blockSize != 0 && (r->opt.blockSize % 32 != 0 || r->opt.blockSize > 256)) {
+        delete r;
+        return fail(OPTPT_ERR_INVALID, "blockSize must be a multiple of 32, at most 256");
+    }
     if (r->opt.leafSize == 0)
         r->opt.leafSize = r->opt.bvhWidth == 8 ? 1 : 4;
     // BVH8 leaves address up to 32 triangles per node with 5-bit offsets.
@@ -756,6 +766,7 @@ int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numV
     if (r->shape.block == 0) {
         const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 128;
         r->shape.block = blk;
+        r->shape.compaction = r->opt.compaction == 1 ? 1 : 0;
         r->shape.gridGenerate = occupancyGrid(0, blk);
         const bool wide = r->bvh.nodes8 != nullptr;
         r->shape.gridExtend = occupancyGrid(wide ? 1 : 11, blk);
@@ -810,7 +821,9 @@ int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numV
     B.views.assign(views, views + numViews);
     B.q.counters = r->q.counters;
     B.q.totals = r->q.totals;
-    int rc = ensureGuideBuffers(r, B.maxPaths);
+    // large batches record one training path in `stride` (about 2^21 per pass)
+    const uint32_t stride = std::max(r->gTrainStride, (B.maxPaths + (1u << 21) - 1) >> 21);
+    int rc = ensureGuideBuffers(r, B.maxPaths, stride);
     if (rc)
         return rc;
     CUDA_OR_RETURN(cudaMemsetAsync(B.acc.sum, 0, sizeof(Acc4) * B.totalPixels, st), "batch");
@@ -826,6 +839,7 @@ int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numV
     if (fp.guide.on) {  // the guiding buffers now hold the batch's paths
         fp.guide.mix = r->gMix;
         fp.guide.rec = r->gRec;
+        fp.guide.trainStride = stride;
     }
     // one captured pass; every replay reads its sizes from the device
     if (!B.exec || B.guideMode != r->guideMode || r->graphDirty) {

@@ -179,6 +179,7 @@ struct AccumBufs {
 struct LaunchShape {
     int gridGenerate, gridExtend, gridShade, gridShadow, gridAccum;
     int block;
+    int compaction;  // shading-queue appends: 0 one atomic per warp, 1 one per block
 };
 
 // wavefront.cu

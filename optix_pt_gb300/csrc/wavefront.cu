@@ -63,6 +63,58 @@ template <int N> OPT_D void warpPush(bool want, uint32_t *counter, float4 *const
     }
 }
 
+// Block-granular compaction of the three shading outputs (continuation,
+// point-light shadow, emissive shadow): one atomicAdd per block and queue.
+// Every thread of the block must call it (trip counts are block-uniform).
+struct BlockPushScratch {
+    uint32_t count[3][8], base[3][8];
+};
+OPT_D void blockPush3(const bool (&want)[3], uint32_t *const (&counter)[3], float4 *const (&d0)[2],
+                      const float4 (&v0)[2], float4 *const (&d1)[3], const float4 (&v1)[3], float4 *const (&d2)[3],
+                      const float4 (&v2)[3], BlockPushScratch &sh)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    unsigned m[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        m[k] = __ballot_sync(0xffffffffu, want[k]);
+        if (lane == 0)
+            sh.count[k][warp] = (uint32_t)__popc(m[k]);
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        uint32_t tot = 0;
+        for (int w = 0; w < nw; ++w) {
+            sh.base[k][w] = tot;
+            tot += sh.count[k][w];
+        }
+        const uint32_t b = tot ? atomicAdd(counter[k], tot) : 0u;
+        for (int w = 0; w < nw; ++w)
+            sh.base[k][w] += b;
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1u;
+    if (want[0]) {
+        const uint32_t slot = sh.base[0][warp] + (uint32_t)__popc(m[0] & below);
+        d0[0][slot] = v0[0];
+        d0[1][slot] = v0[1];
+    }
+    if (want[1]) {
+        const uint32_t slot = sh.base[1][warp] + (uint32_t)__popc(m[1] & below);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            d1[k][slot] = v1[k];
+    }
+    if (want[2]) {
+        const uint32_t slot = sh.base[2][warp] + (uint32_t)__popc(m[2] & below);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            d2[k][slot] = v2[k];
+    }
+    __syncthreads();  // scratch reused by the next iteration
+}
+
 // Alpha test of a candidate (cu/device_programs.cu:108-166 radiance,
 // :180-219 shadow). The any-hit programs interpolate the texture coordinate
 // without the texture transform (:126-130).
@@ -266,7 +318,7 @@ OPT_D float4 texAt(const DevScene &s, int tex, float4 tf, float2 tc)
 // (cu/path_tracer.cu:17-582), miss (cu/device_programs.cu:168-174).
 // GUIDED: the learned-guiding variant (mixture sampling and training
 // records); the plain variant carries none of that code.
-template <bool GUIDED>
+template <bool GUIDED, bool BLOCKPUSH>
 __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBufs q, int depth)
 {
     const uint32_t count = q.counters[CNT_EXT + depth];
@@ -285,8 +337,14 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
     // the estimator unbiased; an untrained proposal should be used sparingly)
     const float ramp = GUIDED ? fminf(1.0f, (float)__ldg(fp.guide.step) / fp.guide.alphaRamp) : 0.0f;
 
-    for (uint32_t base = warpId * 32u; base < count; base += nWarps * 32u) {
-        const uint32_t i = base + (uint32_t)lane;
+    __shared__ BlockPushScratch pushScratch;
+    // warp-granular compaction walks the queue by warps; block-granular by
+    // blocks, so that every thread of a block makes the same number of trips
+    const uint32_t chunk = BLOCKPUSH ? blockDim.x : 32u;
+    const uint32_t first = BLOCKPUSH ? blockIdx.x * blockDim.x : warpId * 32u;
+    const uint32_t step = BLOCKPUSH ? gridDim.x * blockDim.x : nWarps * 32u;
+    for (uint32_t base = first; base < count; base += step) {
+        const uint32_t i = base + (BLOCKPUSH ? threadIdx.x : (uint32_t)lane);
         bool cont = false, wantP = false, wantE = false;
         float4 nxtRay[2], shP[3], shE[3];
         if (i < count) {
@@ -601,9 +659,16 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
             q.pathT[path] = mk4(T, __uint_as_float(flags));
             q.pathL[path] = mk4(L, 0.0f);
         }
-        warpPush<2>(cont, q.counters + CNT_EXT + depth + 1, nextQ, nxtRay);
-        warpPush<3>(wantP, q.counters + CNT_SHADOW_P + depth, shPQ, shP);
-        warpPush<3>(wantE, q.counters + CNT_SHADOW_E + depth, shEQ, shE);
+        if (BLOCKPUSH) {
+            const bool want[3] = {cont, wantP, wantE};
+            uint32_t *const ctrs[3] = {q.counters + CNT_EXT + depth + 1, q.counters + CNT_SHADOW_P + depth,
+                                       q.counters + CNT_SHADOW_E + depth};
+            blockPush3(want, ctrs, nextQ, nxtRay, shPQ, shP, shEQ, shE, pushScratch);
+        } else {
+            warpPush<2>(cont, q.counters + CNT_EXT + depth + 1, nextQ, nxtRay);
+            warpPush<3>(wantP, q.counters + CNT_SHADOW_P + depth, shPQ, shP);
+            warpPush<3>(wantE, q.counters + CNT_SHADOW_E + depth, shEQ, shE);
+        }
     }
 }
 
@@ -846,10 +911,15 @@ void launchExtend(const LaunchShape &ls, const DevScene &s, const FrameParams &f
 void launchShade(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                  cudaStream_t st)
 {
-    if (fp.guide.on)
-        kShade<true><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
+    const bool blockPush = ls.compaction == 1;
+    if (fp.guide.on && blockPush)
+        kShade<true, true><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
+    else if (fp.guide.on)
+        kShade<true, false><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
+    else if (blockPush)
+        kShade<false, true><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
     else
-        kShade<false><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
+        kShade<false, false><<<ls.gridShade, ls.block, 0, st>>>(s, fp, q, depth);
 }
 void launchShadow(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                   int which, cudaStream_t st, bool count)
@@ -894,7 +964,7 @@ int occupancyGrid(int kernelId, int block)
     switch (kernelId) {
     case 0: fn = (const void *)kGenerate; break;
     case 1: fn = (const void *)kExtend<false, true>; break;
-    case 2: fn = (const void *)kShade<false>; break;
+    case 2: fn = (const void *)kShade<false, false>; break;
     case 3: fn = (const void *)kShadow<false, true>; break;
     case 11: fn = (const void *)kExtend<false, false>; break;
     case 13: fn = (const void *)kShadow<false, false>; break;

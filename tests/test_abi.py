@@ -46,7 +46,7 @@ C_PROBE = r"""
 int main(void) {
   S(Light); S(MaterialData); S(LaunchParams); S(optpt_scene); S(optpt_texture); S(optpt_options);
   S(optpt_stats); S(optpt_kernel_times); S(optpt_bsdf_query); S(optpt_bsdf_result); S(TextureTransform);
-  S(optpt_guiding_options); S(optpt_view);
+  S(optpt_guiding_options); S(optpt_view); S(optpt_autotune_request); S(optpt_autotune_trial);
   O(MaterialData, baseColour); O(MaterialData, ior); O(MaterialData, category); O(MaterialData, hasSheenRoughnessTexture);
   O(LaunchParams, traversable); O(LaunchParams, gammaTerm); O(LaunchParams, bgColour);
   O(optpt_scene, camEye); O(optpt_scene, maxDepth); O(optpt_bsdf_query, xs); O(optpt_bsdf_result, pdf);
@@ -73,7 +73,8 @@ def test_struct_layouts_match_c(built):
           "optpt_scene": _ffi.SceneStruct, "optpt_texture": _ffi.Texture, "optpt_options": _ffi.Options,
           "optpt_stats": _ffi.Stats, "optpt_kernel_times": _ffi.KernelTimes,
           "TextureTransform": _ffi.TextureTransform, "optpt_guiding_options": _ffi.GuidingOptions,
-          "optpt_view": _ffi.View}
+          "optpt_view": _ffi.View, "optpt_autotune_request": _ffi.AutotuneRequest,
+          "optpt_autotune_trial": _ffi.AutotuneTrial}
     for name, cls in py.items():
         assert ctypes.sizeof(cls) == c[name], name
     assert _ffi.BSDF_QUERY.itemsize == c["optpt_bsdf_query"]
