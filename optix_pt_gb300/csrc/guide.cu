@@ -82,26 +82,36 @@ __device__ void encodeRow(const GuideGeom &g, const float *hash, const __half *h
 {
     if (valid) {
         const float3 p = unitPos(g, pos);
+        // four levels at a time: their 32 gathers are issued before any is used
 #pragma unroll 1
-        for (int l = 0; l < LEVELS; ++l) {
-            float f0 = 0.0f, f1 = 0.0f;
+        for (int l0 = 0; l0 < LEVELS; l0 += 4) {
+            uint32_t e[4][8];
+            float w[4][8];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                uint32_t e;
-                float w;
-                corner(g.levels, l, p.x, p.y, p.z, c, e, w);
-                const size_t at = ((size_t)l * TABLE + e) * FEATS;
-                if (HALF) {
-                    const __half2 v = *reinterpret_cast<const __half2 *>(hashH + at);
-                    f0 += w * __low2float(v);
-                    f1 += w * __high2float(v);
-                } else {
-                    const float2 v = *reinterpret_cast<const float2 *>(hash + at);
-                    f0 += w * v.x;
-                    f1 += w * v.y;
+            for (int j = 0; j < 4; ++j)
+                levelCorners(g.levels, l0 + j, p.x, p.y, p.z, e[j], w[j]);
+            float2 v[4][8];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const size_t at = ((size_t)(l0 + j) * TABLE + e[j][c]) * FEATS;
+                    if (HALF)
+                        v[j][c] = __half22float2(__ldg(reinterpret_cast<const __half2 *>(hashH + at)));
+                    else
+                        v[j][c] = __ldg(reinterpret_cast<const float2 *>(hash + at));
                 }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    f0 += w[j][c] * v[j][c].x;
+                    f1 += w[j][c] * v[j][c].y;
+                }
+                *reinterpret_cast<__nv_bfloat162 *>(tile + tc::tileOffset(row, 2 * (l0 + j))) =
+                    __floats2bfloat162_rn(f0, f1);
             }
-            *reinterpret_cast<__nv_bfloat162 *>(tile + tc::tileOffset(row, 2 * l)) = __floats2bfloat162_rn(f0, f1);
         }
     } else {
 #pragma unroll
@@ -148,18 +158,41 @@ struct Sync {
     }
 };
 
+// The same for one 128-thread group of a larger CTA, on named barrier `id`.
+struct GroupSync {
+    uint64_t *bar;
+    uint32_t phase;
+    int id;
+    __device__ void toTensor()
+    {
+        tc::fenceProxyAsync();
+        tc::fenceBeforeSync();
+        asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+        tc::fenceAfterSync();
+    }
+    __device__ bool wait()
+    {
+        const bool ok = tc::mbarWait(bar, phase);
+        phase ^= 1u;
+        tc::fenceAfterSync();
+        uint32_t all;
+        asm volatile(
+            "{\n\t.reg .pred q, o;\n\t"
+            "setp.ne.u32 q, %1, 0;\n\t"
+            "bar.red.and.pred o, %2, 128, q;\n\t"
+            "selp.u32 %0, 1, 0, o;\n\t}"
+            : "=r"(all)
+            : "r"(ok ? 1u : 0u), "r"(id)
+            : "memory");
+        return all != 0;
+    }
+};
+
 // This thread's row (64 FP32 columns from col0) of a 128-lane accumulator.
 __device__ __forceinline__ void loadRow(uint32_t tmem, uint32_t col0, float (&v)[WIDTH])
 {
-    const uint32_t lane = (uint32_t)(32 * (threadIdx.x >> 5)) << 16;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        float t[16];
-        tc::ld16(tmem + lane + col0 + 16 * j, t);
-#pragma unroll
-        for (int k = 0; k < 16; ++k)
-            v[16 * j + k] = t[k];
-    }
+    const uint32_t lane = (uint32_t)(32 * ((threadIdx.x >> 5) & 3)) << 16;  // the warp's lane quarter
+    tc::ld64(tmem + lane + col0, v);
 }
 
 // Issues D = X W^T for one 128 x 64 x 64 layer (thread 0 only).
@@ -218,24 +251,29 @@ struct HitInput {
     __device__ void resolve() { n = *countPtr; }
 };
 
-constexpr uint32_t INFER_SMEM = LAYERS * W_BYTES + TILE_BYTES + 1024;
+constexpr uint32_t INFER_SMEM = LAYERS * W_BYTES + 2 * TILE_BYTES + 1024;
 
+// Two 128-row tiles in flight per CTA: threads 0-127 and 128-255 are two
+// groups with their own activation tile, mbarrier, TMEM columns and named
+// barrier, sharing one copy of the weights; while one group waits on its MMA
+// the other gathers or converts.
 template <class In>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 2)
     kGuideInfer(GuideGeom g, const __half *hashH, const uint8_t *tiles, In in, Packed *out, int *status)
 {
     extern __shared__ uint8_t smRaw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smRaw) + 1023) & ~uintptr_t(1023));
-    uint8_t *sW = sm, *sX = sm + LAYERS * W_BYTES;
-    __shared__ uint64_t barLoad, barMma;
+    const int t = threadIdx.x, grp = t >> 7, row = t & 127;
+    uint8_t *sW = sm, *sX = sm + LAYERS * W_BYTES + grp * TILE_BYTES;
+    __shared__ uint64_t barLoad, barMma[2];
     __shared__ uint32_t tmemBase;
-    const int t = threadIdx.x;
     if (t == 0) {
         tc::mbarInit(&barLoad, 1);
-        tc::mbarInit(&barMma, 1);
+        tc::mbarInit(&barMma[0], 1);
+        tc::mbarInit(&barMma[1], 1);
     }
     if (t < 32)
-        tc::tmemAlloc(&tmemBase, 64);
+        tc::tmemAlloc(&tmemBase, 128);
     tc::fenceBeforeSync();
     __syncthreads();
     tc::fenceAfterSync();
@@ -244,21 +282,21 @@ __global__ void __launch_bounds__(128, 1)
         for (int l = 0; l < LAYERS; ++l)
             bulkLoad(sW + l * W_BYTES, tiles + (size_t)l * W_BYTES, W_BYTES, &barLoad);
     }
-    const uint32_t tm = tmemBase;
+    const uint32_t tm = tmemBase + 64u * (uint32_t)grp;
     bool ok = __syncthreads_and(tc::mbarWait(&barLoad, 0) ? 1 : 0) != 0;
-    Sync sync{&barMma, 0};
+    GroupSync sync{&barMma[grp], 0, 1 + grp};
     in.resolve();
     const uint32_t n = in.count();
-    for (uint32_t base = blockIdx.x * TILE_ROWS; ok && base < n; base += gridDim.x * TILE_ROWS) {
+    for (uint32_t base = (blockIdx.x * 2 + grp) * TILE_ROWS; ok && base < n; base += gridDim.x * 2 * TILE_ROWS) {
         float3 p, nrm, wo;
-        const bool valid = in.fetch(base + t, p, nrm, wo);
-        encodeRow<true>(g, nullptr, hashH, p, nrm, wo, valid, sX, t);
+        const bool valid = in.fetch(base + row, p, nrm, wo);
+        encodeRow<true>(g, nullptr, hashH, p, nrm, wo, valid, sX, row);
         float v[WIDTH];
         for (int l = 0; l < LAYERS && ok; ++l) {
             sync.toTensor();
-            if (t == 0) {
+            if (row == 0) {
                 issueLayer(tm, sX, sW + l * W_BYTES);
-                tc::commit(&barMma);
+                tc::commit(&barMma[grp]);
             }
             ok = sync.wait();
             if (!ok)
@@ -271,7 +309,7 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
                     for (int k = 0; k < 8; ++k)
                         r[k] = fmaxf(v[c8 + k], 0.0f);
-                    storeRow8(sX, t, c8, r);  // overwrite: the MMA reading sX has completed
+                    storeRow8(sX, row, c8, r);  // overwrite: the MMA reading sX has completed
                 }
             }
         }
@@ -280,16 +318,16 @@ __global__ void __launch_bounds__(128, 1)
             decodeOutputs(v, m);
             Packed pk;
             pack(m, pk);
-            out[base + t] = pk;
+            out[base + row] = pk;
         }
     }
-    if (!ok && t == 0)
+    if (!ok && row == 0)
         atomicExch(status, 1);
     tc::fenceBeforeSync();
     __syncthreads();
     tc::fenceAfterSync();
     if (t < 32)
-        tc::tmemFree(tm, 64);
+        tc::tmemFree(tmemBase, 128);
 }
 
 // ------------------------------------------------------------------ training
@@ -779,8 +817,8 @@ cudaError_t guideInferQueries(const optpt_guide *g, const GuideQuery *q, uint32_
     if (n == 0)
         return cudaSuccess;
     const int tiles = (int)((n + TILE_ROWS - 1) / TILE_ROWS);
-    const int grid = std::min(tiles, g->numSMs * 2);
-    kGuideInfer<QueryInput><<<grid, 128, INFER_SMEM, s>>>(guideGeom(g), g->hashH, g->tiles, QueryInput{q, n}, out,
+    const int grid = std::min((tiles + 1) / 2, g->numSMs * 2);
+    kGuideInfer<QueryInput><<<grid, 256, INFER_SMEM, s>>>(guideGeom(g), g->hashH, g->tiles, QueryInput{q, n}, out,
                                                           g->status);
     return cudaGetLastError();
 }
@@ -814,7 +852,7 @@ void launchGuideInfer(const optpt_guide *g, const DevScene &sc, const FrameParam
 {
     const int cur = depth & 1;
     HitInput in{q.rayO[cur], q.rayD[cur], q.hit, sc.triV, q.counters + CNT_EXT + depth, 0u};
-    kGuideInfer<HitInput><<<g->numSMs * 3, 128, INFER_SMEM, st>>>(
+    kGuideInfer<HitInput><<<g->numSMs * 2, 256, INFER_SMEM, st>>>(
         guideGeom(g), g->hashH, g->tiles, in, reinterpret_cast<Packed *>(const_cast<void *>(fp.guide.mix)),
         g->status);
 }

@@ -52,6 +52,23 @@ OPT_HD void corner(const Levels &L, int l, float px, float py, float pz, int c, 
     entry = cornerIndex(x, y, z, (uint32_t)r + 1u, L.dense[l] != 0);
 }
 
+// All 8 trilinear corners of level `l` (the same arithmetic as `corner`,
+// with the cell computed once).
+OPT_HD void levelCorners(const Levels &L, int l, float px, float py, float pz, uint32_t (&entry)[8], float (&w)[8])
+{
+    const float r = L.res[l];
+    const float gx = px * r, gy = py * r, gz = pz * r;
+    const float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    const float tx = gx - fx, ty = gy - fy, tz = gz - fz;
+    const uint32_t x0 = (uint32_t)fx, y0 = (uint32_t)fy, z0 = (uint32_t)fz, res1 = (uint32_t)r + 1u;
+    const bool dense = L.dense[l] != 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        w[c] = ((c & 1) ? tx : 1.0f - tx) * (((c >> 1) & 1) ? ty : 1.0f - ty) * (((c >> 2) & 1) ? tz : 1.0f - tz);
+        entry[c] = cornerIndex(x0 + (c & 1), y0 + ((c >> 1) & 1), z0 + ((c >> 2) & 1), res1, dense);
+    }
+}
+
 // ------------------------------------------------------------------ vMF mixture
 struct Lobe {
     float3 mu;
