@@ -199,6 +199,13 @@ typedef struct optpt_kernel_times {
 } optpt_kernel_times;
 int optpt_render_profiled(optpt_renderer *r, uint32_t spp, void *stream, optpt_kernel_times *out);
 
+/* Queue lengths of the last pass, per bounce d = 1..maxDepth (host arrays of
+ * maxDepth entries, any may be NULL): extension rays, point-light and
+ * emissive-triangle shadow rays. For relating a profiled launch to the rays
+ * it traced; the reference has no counterpart (OptiX hides its queues). */
+int optpt_queue_counts(optpt_renderer *r, uint32_t *ext, uint32_t *shadowPoint, uint32_t *shadowEmissive,
+                       uint32_t maxDepth);
+
 /* BVH work of one extra render of `spp` samples, run with counting variants
  * of the traversal kernels (slower; not for timing): rays traced, BVH nodes
  * visited and triangles tested, for extension and shadow rays. Feeds the

@@ -264,6 +264,13 @@ class Renderer:
         return {"ms": dict(zip(names, list(kt.ms))), "launches": dict(zip(names, list(kt.launches))),
                 "extensionRays": kt.extensionRays, "shadowRays": kt.shadowRays}
 
+    def queue_counts(self):
+        """Per-bounce queue lengths of the last pass: (extension, point shadow, emissive shadow)."""
+        d = self.launch_params().maxDepth
+        a, b, c = (np.zeros(d, np.uint32) for _ in range(3))
+        check(lib.optpt_queue_counts(self._h, a.ctypes.data, b.ctypes.data, c.ctypes.data, d))
+        return a, b, c
+
     def traversal_counts(self, spp, stream=None):
         c = _ffi.TraversalCounts()
         check(lib.optpt_traversal_counts(self._h, spp, _stream_handle(stream), ctypes.byref(c)))

@@ -196,6 +196,7 @@ _sigs = {
                                           ctypes.POINTER(ctypes.c_double)]),
     "optpt_set_guiding": (ctypes.c_int, [_H, ctypes.c_int]),
     "optpt_get_guide": (ctypes.c_int, [_H, ctypes.POINTER(_P)]),
+    "optpt_queue_counts": (ctypes.c_int, [_H, _P, _P, _P, ctypes.c_uint32]),
     "optpt_guiding_batch": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
     "optpt_render_batch": (ctypes.c_int, [_H, ctypes.POINTER(View), ctypes.c_uint32, _P]),
     "optpt_autotune": (ctypes.c_int, [ctypes.POINTER(SceneStruct), ctypes.POINTER(AutotuneRequest),

@@ -1042,6 +1042,27 @@ int optpt_guiding_batch(optpt_renderer *r, float *samples, uint32_t capacity, ui
     return OPTPT_OK;
 }
 
+int optpt_queue_counts(optpt_renderer *r, uint32_t *ext, uint32_t *shadowPoint, uint32_t *shadowEmissive,
+                       uint32_t maxDepth)
+{
+    if (!r)
+        return fail(OPTPT_ERR_INVALID, "NULL renderer");
+    if (maxDepth > OPT_MAX_DEPTH)
+        return fail(OPTPT_ERR_INVALID, "maxDepth out of range");
+    uint32_t c[CNT_TOTAL];
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "queue counts");
+    CUDA_OR_RETURN(cudaMemcpy(c, r->q.counters, sizeof(c), cudaMemcpyDeviceToHost), "queue counts");
+    for (uint32_t d = 1; d <= maxDepth; ++d) {
+        if (ext)
+            ext[d - 1] = c[CNT_EXT + d];
+        if (shadowPoint)
+            shadowPoint[d - 1] = c[CNT_SHADOW_P + d];
+        if (shadowEmissive)
+            shadowEmissive[d - 1] = c[CNT_SHADOW_E + d];
+    }
+    return OPTPT_OK;
+}
+
 int optpt_get_guide(optpt_renderer *r, optpt_guide **out)
 {
     if (!r || !out)

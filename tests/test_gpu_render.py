@@ -161,3 +161,27 @@ def test_api_errors(cuda_dev):
     with pytest.raises(opt.OptptError):
         opt.Renderer(bad)
     r.close()
+
+
+def test_queue_counts_match_ray_totals(cuda_dev):
+    """Per-bounce queue lengths of the last pass add up to the rays that pass
+    traced; the first bounce holds one camera ray per pixel."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    r = opt.Renderer(sc)
+    r.setupOutputBuffer(64, 48)
+    r.render(1, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    s0 = r.stats()
+    r.render(1, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    s1 = r.stats()
+    e, p, m = r.queue_counts()
+    assert len(e) == r.launch_params().maxDepth
+    assert e[0] == 64 * 48
+    assert (np.diff(e.astype(np.int64)) <= 0).all()
+    assert int(e.sum()) == s1["extensionRays"] - s0["extensionRays"]
+    assert int(p.sum()) + int(m.sum()) == s1["shadowRays"] - s0["shadowRays"]
+    r.close()
