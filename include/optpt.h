@@ -46,7 +46,8 @@ int optpt_version(void);
 /* ------------------------------------------------------------------ scene */
 
 /* An RGBA8 texture image. wrap: 0 repeat, 1 clamp, 2 mirror. srgb: decode
- * the colour channels from sRGB (reference: src/renderer.cpp:1471-1483). */
+ * the colour channels from sRGB. filter: 0 bilinear, 1 nearest (the
+ * reference's cudaFilterModeLinear / Point, src/renderer.cpp:1471-1530). */
 typedef struct optpt_texture {
     uint32_t width;
     uint32_t height;
@@ -54,7 +55,7 @@ typedef struct optpt_texture {
     int32_t wrapS;
     int32_t wrapT;
     int32_t srgb;
-    int32_t pad;
+    int32_t filter;
 } optpt_texture;
 
 /* A flattened, world-space triangle scene plus camera and frame settings:
@@ -96,10 +97,40 @@ void optpt_scene_release(optpt_scene *scene);
 /* Resolves a scene-selection list in the reference's configs/<name>.json format
  * (src/scene_desc.cpp:118-153: {"scene": id, id: name}) and parses the named
  * scene file (src/scene_desc.cpp:50-116). A scene file names either
- * "gltf scene file" (not supported: returns OPTPT_ERR_INVALID) or
- * "procedural scene"; "renderer.dimensions" and "renderer.background colour"
- * override the scene's defaults. */
+ * "gltf scene file" (imported with optpt_scene_from_gltf; a relative path is
+ * tried against the working directory, as the reference opens it, then
+ * against the scene file's directory; "gltf up hint" sets the camera's up
+ * vector) or "procedural scene"; "renderer.dimensions" and
+ * "renderer.background colour" override the scene's defaults. */
 int optpt_scene_from_config(const char *sceneListPath, optpt_scene *out);
+
+/* Imports a glTF 2.0 scene (.gltf with external or data-URI buffers, or a
+ * binary .glb) into library-owned host arrays (released with
+ * optpt_scene_release), as the reference's GltfLoader::parse/loadScene and
+ * Renderer::loadScene/updateScene do (src/gltf_loader.cpp:19-1388,
+ * src/renderer.cpp:191-265,1060-1303): the default scene's mesh nodes
+ * flattened to world space, materials with KHR_materials_{specular,
+ * transmission, ior, emissive_strength, clearcoat, sheen} and
+ * KHR_texture_transform, PNG textures decoded to RGBA8, KHR_lights_punctual
+ * lights and the first perspective camera. upHint may be NULL ((0, 1, 0)).
+ * Frame defaults: 1280 x 720, 64 spp, depth 8. Errors: OPTPT_ERR_IO for an
+ * unreadable file, OPTPT_ERR_PARSE for malformed JSON, buffers or images. */
+int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *out);
+
+/* An RGBA8 image in library-owned memory. */
+typedef struct optpt_image {
+    uint32_t width;
+    uint32_t height;
+    uint8_t *rgba;
+} optpt_image;
+
+/* Decodes a PNG held in memory to RGBA8 with stb_image's four-component
+ * rules (the decoder tinygltf runs for the reference): grey expands to RGB,
+ * missing alpha is 255, 16-bit samples keep their high byte, palettes and
+ * tRNS apply, Adam7 interlacing is undone. OPTPT_ERR_PARSE on a malformed or
+ * truncated file (CRC and Adler-32 checked). */
+int optpt_image_decode_png(const void *data, size_t size, optpt_image *out);
+void optpt_image_release(optpt_image *img);
 
 /* ------------------------------------------------------------------ renderer */
 

@@ -15,7 +15,7 @@ import numpy as np
 from . import _ffi
 from ._ffi import BSDF_QUERY, BSDF_RESULT, OptptError, check, lib
 
-__all__ = ["Scene", "SceneDesc", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
+__all__ = ["Scene", "SceneDesc", "decode_png", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
            "library_path"]
 
 library_path = _ffi.LIB_PATH
@@ -47,6 +47,31 @@ class Scene:
         s = _ffi.SceneStruct()
         check(lib.optpt_scene_from_config(str(scene_list_path).encode(), ctypes.byref(s)))
         return cls(s, True)
+
+    @classmethod
+    def from_gltf(cls, path, up=(0.0, 1.0, 0.0)):
+        """Imports a glTF 2.0 file (.gltf or .glb): GltfLoader + Renderer::loadScene."""
+        s = _ffi.SceneStruct()
+        u = (ctypes.c_float * 3)(*up)
+        check(lib.optpt_scene_from_gltf(str(path).encode(), ctypes.cast(u, ctypes.c_void_p), ctypes.byref(s)))
+        return cls(s, True)
+
+    def textures(self):
+        """Copies of the texture images: list of dicts (rgba HxWx4 uint8, wrapS, wrapT, srgb, filter)."""
+        out = []
+        for t in range(self._s.numTextures):
+            tx = self._s.textures[t]
+            px = np.ctypeslib.as_array(ctypes.cast(tx.rgba, ctypes.POINTER(ctypes.c_uint8)),
+                                       shape=(tx.height * tx.width * 4,)).copy().reshape(tx.height, tx.width, 4)
+            out.append({"rgba": px, "wrapS": tx.wrapS, "wrapT": tx.wrapT, "srgb": tx.srgb, "filter": tx.filter})
+        return out
+
+    def materials(self):
+        """The MaterialData records as a list of ctypes structures (copies)."""
+        return [_ffi.MaterialData.from_buffer_copy(self._s.materials[i]) for i in range(self._s.numMaterials)]
+
+    def lights(self):
+        return [_ffi.Light.from_buffer_copy(self._s.lights[i]) for i in range(self._s.numLights)]
 
     def __del__(self):
         if getattr(self, "_owned", False):
@@ -86,6 +111,18 @@ class Scene:
             "spp": s.spp, "maxDepth": s.maxDepth,
         }
         return out
+
+
+def decode_png(data):
+    """Decodes PNG bytes to an HxWx4 uint8 array with the library's decoder."""
+    img = _ffi.Image()
+    buf = ctypes.create_string_buffer(bytes(data), len(data))
+    check(lib.optpt_image_decode_png(buf, len(data), ctypes.byref(img)))
+    try:
+        return np.ctypeslib.as_array(img.rgba, shape=(img.height * img.width * 4,)).copy().reshape(
+            img.height, img.width, 4)
+    finally:
+        lib.optpt_image_release(ctypes.byref(img))
 
 
 SceneDesc = Scene.from_config  # the reference constructs SceneDesc from the scene list

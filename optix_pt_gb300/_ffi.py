@@ -79,7 +79,11 @@ class LaunchParams(ctypes.Structure):
 class Texture(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("rgba", ctypes.c_void_p),
                 ("wrapS", ctypes.c_int32), ("wrapT", ctypes.c_int32), ("srgb", ctypes.c_int32),
-                ("pad", ctypes.c_int32)]
+                ("filter", ctypes.c_int32)]
+
+
+class Image(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("rgba", ctypes.POINTER(ctypes.c_uint8))]
 
 
 class SceneStruct(ctypes.Structure):
@@ -158,6 +162,9 @@ _sigs = {
     "optpt_scene_procedural": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, ctypes.POINTER(SceneStruct)]),
     "optpt_scene_release": (None, [ctypes.POINTER(SceneStruct)]),
     "optpt_scene_from_config": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(SceneStruct)]),
+    "optpt_scene_from_gltf": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.POINTER(SceneStruct)]),
+    "optpt_image_decode_png": (ctypes.c_int, [_P, ctypes.c_size_t, ctypes.POINTER(Image)]),
+    "optpt_image_release": (None, [ctypes.POINTER(Image)]),
     "optpt_create": (ctypes.c_int, [ctypes.POINTER(SceneStruct), ctypes.POINTER(Options), ctypes.POINTER(_H)]),
     "optpt_destroy": (ctypes.c_int, [_H]),
     "optpt_setup_output_buffer": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32]),

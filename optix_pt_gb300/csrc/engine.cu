@@ -659,7 +659,8 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
             texels.resize(texels.size() + cnt);
             memcpy(texels.data() + first, tx.rgba, cnt * 4);
             texInfo.push_back(make_int4(first, (int)tx.width, (int)tx.height,
-                                        (tx.wrapS & 0xF) | ((tx.wrapT & 0xF) << 4) | ((tx.srgb ? 1 : 0) << 8)));
+                                        (tx.wrapS & 0xF) | ((tx.wrapT & 0xF) << 4) | ((tx.srgb ? 1 : 0) << 8) |
+                                            ((tx.filter == 1 ? 1 : 0) << 9)));
         }
         if ((e = upload(r->dPositions, s->positions, (size_t)3 * s->numVertices)) ||
             (e = upload(r->dNormals, s->normals, s->normals ? (size_t)3 * s->numVertices : 0)) ||

@@ -1,0 +1,35 @@
+// Project-written image codecs for scene import and frame output: zlib
+// inflate (RFC 1950/1951), PNG decoding to RGBA8 (PNG 1.2: every colour type
+// and bit depth, palette and tRNS transparency, Adam7 interlacing), and the
+// CRC-32 / Adler-32 checksums PNG and zlib carry. The reference reads images
+// through stb_image inside tinygltf (src/gltf_loader.cpp:532) and writes them
+// through stb_image_write / OpenEXR; neither library is available here.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace optimg {
+
+uint32_t crc32(const uint8_t *p, size_t n, uint32_t crc = 0);
+uint32_t adler32(const uint8_t *p, size_t n, uint32_t a = 1);
+
+// Raw DEFLATE stream -> bytes. Fails (returns false, message in err) on a
+// malformed stream or when the output would exceed maxOut bytes.
+bool inflate(const uint8_t *in, size_t n, std::vector<uint8_t> &out, size_t maxOut, std::string &err);
+// zlib stream (header, DEFLATE data, Adler-32 trailer) -> bytes.
+bool zlibDecompress(const uint8_t *in, size_t n, std::vector<uint8_t> &out, size_t maxOut, std::string &err);
+
+struct Image {
+    uint32_t width = 0, height = 0;
+    std::vector<uint8_t> rgba;  // width * height * 4, rows top to bottom
+};
+
+bool isPng(const uint8_t *p, size_t n);
+// Decodes a PNG to RGBA8 as stb_image does with four requested components:
+// grey expands to (g, g, g), missing alpha is 255, 16-bit samples keep their
+// high byte, low bit depths scale to 0..255, palette and tRNS apply.
+bool decodePng(const uint8_t *p, size_t n, Image &img, std::string &err);
+
+}  // namespace optimg

@@ -18,8 +18,12 @@
 #include <string>
 #include <vector>
 #include "../../include/optpt.h"
+#include "host_scene.h"
+#include "json.h"
 
 extern "C" int optpt_internal_set_error(int code, const char *msg);
+
+using namespace optjson;
 
 namespace {
 
@@ -50,6 +54,10 @@ struct SceneRng {
     double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
     double range(double a, double b) { return a + (b - a) * uniform(); }
 };
+
+}  // namespace
+
+namespace opthost {
 
 // MaterialParams::isDeterministic / categorise (include/material_params.h:
 // 116-223 of the reference): materials without any per-hit choice get their
@@ -132,6 +140,12 @@ MaterialData baseMaterial(double r, double g, double b)
     m.specular = 0.0f;
     return m;
 }
+
+}  // namespace opthost
+
+using namespace opthost;
+
+namespace {
 
 struct Builder {
     std::vector<float> pos, nrm, tc;
@@ -708,193 +722,6 @@ int buildInterior(uint32_t seed, int balls, int subdiv, optpt_scene *out)
     return OPTPT_OK;
 }
 
-// ------------------------------------------------------------------ JSON
-// A small recursive-descent JSON reader for the scene-selection files (the
-// reference uses rapidjson, src/scene_desc.cpp:50-153).
-struct Json {
-    enum Type { Null, Bool, Num, Str, Arr, Obj } type = Null;
-    double num = 0;
-    bool b = false;
-    std::string str;
-    std::vector<Json> arr;
-    std::vector<std::pair<std::string, Json>> obj;
-    const Json *get(const std::string &k) const
-    {
-        for (auto &kv : obj)
-            if (kv.first == k)
-                return &kv.second;
-        return nullptr;
-    }
-};
-
-struct JsonParser {
-    const std::string &s;
-    size_t i = 0;
-    std::string err;
-    explicit JsonParser(const std::string &src) : s(src) {}
-    void ws()
-    {
-        while (i < s.size() && (s[i] == ' ' || s[i] == '\t' || s[i] == '\n' || s[i] == '\r'))
-            ++i;
-    }
-    bool fail(const char *m)
-    {
-        if (err.empty())
-            err = std::string(m) + " at offset " + std::to_string(i);
-        return false;
-    }
-    bool value(Json &v, int depth)
-    {
-        if (depth > 64)
-            return fail("nesting too deep");
-        ws();
-        if (i >= s.size())
-            return fail("unexpected end");
-        char c = s[i];
-        if (c == '{') {
-            v.type = Json::Obj;
-            ++i;
-            ws();
-            if (i < s.size() && s[i] == '}') {
-                ++i;
-                return true;
-            }
-            while (true) {
-                ws();
-                Json k;
-                if (i >= s.size() || s[i] != '"' || !string(k.str))
-                    return fail("expected member name");
-                ws();
-                if (i >= s.size() || s[i] != ':')
-                    return fail("expected ':'");
-                ++i;
-                Json val;
-                if (!value(val, depth + 1))
-                    return false;
-                v.obj.emplace_back(k.str, std::move(val));
-                ws();
-                if (i < s.size() && s[i] == ',') {
-                    ++i;
-                    continue;
-                }
-                if (i < s.size() && s[i] == '}') {
-                    ++i;
-                    return true;
-                }
-                return fail("expected ',' or '}'");
-            }
-        }
-        if (c == '[') {
-            v.type = Json::Arr;
-            ++i;
-            ws();
-            if (i < s.size() && s[i] == ']') {
-                ++i;
-                return true;
-            }
-            while (true) {
-                Json val;
-                if (!value(val, depth + 1))
-                    return false;
-                v.arr.push_back(std::move(val));
-                ws();
-                if (i < s.size() && s[i] == ',') {
-                    ++i;
-                    continue;
-                }
-                if (i < s.size() && s[i] == ']') {
-                    ++i;
-                    return true;
-                }
-                return fail("expected ',' or ']'");
-            }
-        }
-        if (c == '"') {
-            v.type = Json::Str;
-            return string(v.str);
-        }
-        if (s.compare(i, 4, "true") == 0) {
-            v.type = Json::Bool;
-            v.b = true;
-            i += 4;
-            return true;
-        }
-        if (s.compare(i, 5, "false") == 0) {
-            v.type = Json::Bool;
-            i += 5;
-            return true;
-        }
-        if (s.compare(i, 4, "null") == 0) {
-            i += 4;
-            return true;
-        }
-        if (c == '-' || (c >= '0' && c <= '9')) {
-            const char *b0 = s.c_str() + i;
-            char *e = nullptr;
-            v.num = std::strtod(b0, &e);
-            if (e == b0)
-                return fail("bad number");
-            v.type = Json::Num;
-            i += (size_t)(e - b0);
-            return true;
-        }
-        return fail("unexpected character");
-    }
-    bool string(std::string &out)
-    {
-        ++i;  // opening quote
-        while (i < s.size() && s[i] != '"') {
-            if (s[i] == '\\') {
-                if (i + 1 >= s.size())
-                    return fail("bad escape");
-                char e = s[i + 1];
-                out.push_back(e == 'n' ? '\n' : e == 't' ? '\t' : e);
-                i += 2;
-            } else {
-                out.push_back(s[i++]);
-            }
-        }
-        if (i >= s.size())
-            return fail("missing closing quote");
-        ++i;
-        return true;
-    }
-};
-
-bool readFile(const std::string &path, std::string &out)
-{
-    std::ifstream f(path, std::ios::binary);
-    if (!f)
-        return false;
-    std::stringstream ss;
-    ss << f.rdbuf();
-    out = ss.str();
-    return !out.empty();
-}
-
-int parseJson(const std::string &text, Json &out, const std::string &what)
-{
-    JsonParser p(text);
-    if (!p.value(out, 0))
-        return optpt_internal_set_error(OPTPT_ERR_PARSE, ("error parsing " + what + ": " + p.err).c_str());
-    p.ws();
-    if (p.i != text.size())
-        return optpt_internal_set_error(OPTPT_ERR_PARSE, ("error parsing " + what + ": trailing characters").c_str());
-    return OPTPT_OK;
-}
-
-bool vec3(const Json *j, float *d)
-{
-    if (!j || j->type != Json::Arr || j->arr.size() != 3)
-        return false;
-    for (int k = 0; k < 3; ++k) {
-        if (j->arr[k].type != Json::Num)
-            return false;
-        d[k] = (float)j->arr[k].num;
-    }
-    return true;
-}
-
 }  // namespace
 
 extern "C" {
@@ -972,17 +799,31 @@ int optpt_scene_from_config(const char *sceneListPath, optpt_scene *out)
     if (!scene || scene->type != Json::Obj)
         return optpt_internal_set_error(OPTPT_ERR_PARSE, "object \"scene\" not found");
     const Json *proc = scene->get("procedural scene");
-    if (!proc || proc->type != Json::Str) {
-        if (scene->get("gltf scene file"))
-            return optpt_internal_set_error(OPTPT_ERR_INVALID, "glTF scene files are not supported; use \"procedural scene\"");
+    const Json *gltf = scene->get("gltf scene file");
+    if (proc && proc->type == Json::Str) {
+        uint32_t seed = 1;
+        if (const Json *sd = scene->get("seed"))
+            if (sd->type == Json::Num)
+                seed = (uint32_t)sd->num;
+        if ((rc = optpt_scene_procedural(proc->str.c_str(), seed, out)))
+            return rc;
+    } else if (gltf && gltf->type == Json::Str) {
+        // SceneDesc::parseGltfScene (src/scene_desc.cpp:78-93): the file as
+        // given (the reference opens it relative to the working directory),
+        // else relative to this scene file; up hint default (0, 1, 0).
+        float up[3] = {0.0f, 1.0f, 0.0f};
+        if (const Json *uh = scene->get("gltf up hint"))
+            if (!vec3(uh, up))
+                return optpt_internal_set_error(OPTPT_ERR_PARSE, "\"gltf up hint\" must be [x, y, z]");
+        std::string path = gltf->str, probe;
+        const bool absolute = !path.empty() && (path[0] == '/' || path[0] == '\\');
+        if (!absolute && !readFile(path, probe) && readFile(dir + path, probe))
+            path = dir + path;
+        if ((rc = optpt_scene_from_gltf(path.c_str(), up, out)))
+            return rc;
+    } else {
         return optpt_internal_set_error(OPTPT_ERR_PARSE, "no scene source in \"scene\"");
     }
-    uint32_t seed = 1;
-    if (const Json *sd = scene->get("seed"))
-        if (sd->type == Json::Num)
-            seed = (uint32_t)sd->num;
-    if ((rc = optpt_scene_procedural(proc->str.c_str(), seed, out)))
-        return rc;
     const Json *ren = scene->get("renderer");
     if (!ren || ren->type != Json::Obj) {
         optpt_scene_release(out);

@@ -693,6 +693,14 @@ float sampleTex(const SceneView &sv, int tex, float u, float v, float out[4])
 {
     const optpt_texture &t = sv.s->textures[tex];
     const int W = (int)t.width, H = (int)t.height;
+    if (t.filter == 1) {
+        // Nearest texel (cudaFilterModePoint): floor(u * W), floor(v * H).
+        const int px = wrapTexel((int)std::floor(u * (float)W), W, t.wrapS);
+        const int py = wrapTexel((int)std::floor(v * (float)H), H, t.wrapT);
+        for (int c = 0; c < 4; ++c)
+            out[c] = texChan(sv, t, px, py, c);
+        return out[3];
+    }
     const float x = std::fma(u, (float)W, -0.5f), y = std::fma(v, (float)H, -0.5f);
     float fx0 = std::floor(x), fy0 = std::floor(y);
     float ax = x - fx0, ay = y - fy0;

@@ -71,7 +71,7 @@ def test_config_selection(built, tmp_path):
 
 
 @pytest.mark.parametrize("case,code", [
-    ("missing_list", -3), ("bad_json", -4), ("no_id", -4), ("gltf", -1), ("no_renderer", -4), ("missing_scene", -3),
+    ("missing_list", -3), ("bad_json", -4), ("no_id", -4), ("gltf", -3), ("no_renderer", -4), ("missing_scene", -3),
 ])
 def test_config_errors(built, tmp_path, case, code):
     import optix_pt_gb300 as opt
