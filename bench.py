@@ -285,6 +285,32 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def image_output_measure(r, peak, reps=20):
+    """The fused frame-output kernel (RGBA8 + RGBE + HALF payloads in one
+    pass) on this frame: CUDA-event time per launch with L2 flushed before
+    each, against 48 algorithmic bytes per pixel (two float4 reads, 16 B of
+    payload writes); plus wall time of each file dump through the public API
+    (GPU payload, copy, host encoding, write)."""
+    import tempfile
+
+    lp = r.launch_params()
+    n = lp.w * lp.h
+    ms = r.image_out_profile(reps)  # events recorded by the library around each launch
+    achieved = 48.0 * n / (ms / 1e3) / 1e9
+    dumps = {}
+    with tempfile.TemporaryDirectory() as d:
+        for name, fn in (("png", r.dumpFramebuffer), ("hdr", r.dumpAccumFramebufferRgbe),
+                         ("exr_zip", r.dumpAccumFramebufferExr)):
+            path = os.path.join(d, "out." + name)
+            fn(path)  # warm
+            t0 = time.perf_counter()
+            fn(path)
+            dumps[name] = {"ms": (time.perf_counter() - t0) * 1e3, "bytes": os.path.getsize(path)}
+    return {"kernel": "kImageOut", "pixels": n, "bytes_per_pixel": 48, "ms_per_launch": ms,
+            "achieved_gbs": achieved, "peak_gbs": peak, "frac": achieved / peak,
+            "l2": "flushed before each launch", "dump_wall": dumps}
+
+
 def run_reference(args, rank, world):
     """The reference arm: the oracle integrator on the host cores."""
     if rank != 0:
@@ -440,6 +466,8 @@ def run_ours(args, rank, world, local_rank):
                 "kernel_ms_per_pass": {k: v / 2 for k, v in kms.items()},
                 "kernel_share": {k: v / sum(kms.values()) for k, v in kms.items()}}
 
+    image_output = image_output_measure(r, peak) if world == 1 else None
+
     guided = None
     if world == 1 and not args.no_guided:
         guided = guided_equal_time(stream, args.guided_budget, args.guided_ref_spp)
@@ -465,7 +493,7 @@ def run_ours(args, rank, world, local_rank):
                     "d2h_bytes_per_step": w * h * 16},
             "gpu_launches": passes_launches * args.steps,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "guided_vs_plain_equal_time": guided}
+            "guided_vs_plain_equal_time": guided, "image_output": image_output}
     print(json.dumps(line))
     r.close()
 

@@ -202,6 +202,50 @@ int optpt_read_frame_buffer(optpt_renderer *r, float *rgbaHost, void *stream);
  * w*h each) to caller host memory, ordered on `stream`, and waits for it. */
 int optpt_read_accum(optpt_renderer *r, double *sumHost, double *sumSqHost, void *stream);
 
+/* ------------------------------------------------------------------ image output */
+
+/* One GPU pass over the current frame producing the image writers' payloads
+ * into caller DEVICE buffers (any may be NULL), ordered on `stream`:
+ *   rgba8    w*h uint32: processImage (cu/kernels.cu:22-33) of the tone-mapped
+ *            frame buffer, 0xff000000 | r | g << 8 | b << 16 with
+ *            r = int(clamp(255.99 x, 0, 255));
+ *   rgbe     w*h uint32: Ward RGBE of the accumulated mean radiance (bytes
+ *            r, g, b, exponent + 128), as stbi_write_hdr stores it;
+ *   halfRows w*h*4 IEEE halves of the accumulated mean with A = 1, each
+ *            scanline channel-planar A[w], B[w], G[w], R[w] (an OpenEXR
+ *            scanline's layout), rounded to nearest even. */
+int optpt_image_out(optpt_renderer *r, uint32_t *rgba8, uint32_t *rgbe, void *halfRows, void *stream);
+
+/* Average CUDA-event time of the output kernel producing all three payloads
+ * into library scratch, each of `reps` launches preceded by a 256 MB write
+ * that evicts L2 (for roofline measurement). */
+int optpt_image_out_profiled(optpt_renderer *r, uint32_t reps, float *msPerLaunch);
+
+/* processImage's RGBA8 copied to caller host memory (w*h uint32, rows top
+ * to bottom), ordered on `stream`; waits for it. */
+int optpt_read_rgba8(optpt_renderer *r, uint32_t *rgbaHost, void *stream);
+
+/* Writes the current frame to a file, replacing Renderer::dumpFramebuffer,
+ * dumpAccumFramebufferRgbe and the EXR dump (src/renderer.cpp:1001-1026,
+ * 1361-1370): format 0 PNG (RGBA8 of processImage), 1 Radiance .hdr
+ * (run-length encoded RGBE of the accumulated mean), 2 OpenEXR (HALF RGBA of
+ * the accumulated mean, A = 1, ZIP compression). path NULL writes the
+ * reference's names output.png / output.hdr / output.exr in the working
+ * directory. Waits for all GPU work first. */
+int optpt_save_image(optpt_renderer *r, int format, const char *path);
+
+/* Host-side encoders for images already in host memory; the encoded file is
+ * returned in library-owned memory released with optpt_free.
+ *   optpt_encode_png: RGBA8 rows (strideBytes 0 = width * 4);
+ *   optpt_encode_hdr: float RGBA pixels to run-length RGBE;
+ *   optpt_encode_exr: float RGBA pixels to HALF A, B, G, R with A = 1;
+ *                     compression 0 none, 3 ZIP. */
+int optpt_encode_png(const uint8_t *rgba, uint32_t width, uint32_t height, size_t strideBytes, void **out,
+                     size_t *size);
+int optpt_encode_hdr(const float *rgba, uint32_t width, uint32_t height, void **out, size_t *size);
+int optpt_encode_exr(const float *rgba, uint32_t width, uint32_t height, int compression, void **out, size_t *size);
+void optpt_free(void *p);
+
 /* Counters accumulated since creation (read after the GPU work finished). */
 typedef struct optpt_stats {
     uint64_t extensionRays;  /* rays traced by the closest-hit kernel   */

@@ -15,7 +15,7 @@ import numpy as np
 from . import _ffi
 from ._ffi import BSDF_QUERY, BSDF_RESULT, OptptError, check, lib
 
-__all__ = ["Scene", "SceneDesc", "decode_png", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
+__all__ = ["Scene", "SceneDesc", "decode_png", "encode_png", "encode_hdr", "encode_exr", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
            "library_path"]
 
 library_path = _ffi.LIB_PATH
@@ -123,6 +123,33 @@ def decode_png(data):
             img.height, img.width, 4)
     finally:
         lib.optpt_image_release(ctypes.byref(img))
+
+
+def _encoded(fn, *args):
+    out, size = ctypes.c_void_p(), ctypes.c_size_t()
+    check(fn(*args, ctypes.byref(out), ctypes.byref(size)))
+    try:
+        return ctypes.string_at(out.value, size.value)
+    finally:
+        lib.optpt_free(out)
+
+
+def encode_png(rgba):
+    """(h, w, 4) uint8 -> PNG bytes (the library's encoder)."""
+    a = np.ascontiguousarray(rgba, np.uint8)
+    return _encoded(lib.optpt_encode_png, a.ctypes.data, a.shape[1], a.shape[0], a.shape[1] * 4)
+
+
+def encode_hdr(rgba):
+    """(h, w, 4) float32 -> Radiance RGBE bytes."""
+    a = np.ascontiguousarray(rgba, np.float32)
+    return _encoded(lib.optpt_encode_hdr, a.ctypes.data, a.shape[1], a.shape[0])
+
+
+def encode_exr(rgba, compression=3):
+    """(h, w, 4) float32 -> OpenEXR bytes (HALF A, B, G, R; A = 1)."""
+    a = np.ascontiguousarray(rgba, np.float32)
+    return _encoded(lib.optpt_encode_exr, a.ctypes.data, a.shape[1], a.shape[0], compression)
 
 
 SceneDesc = Scene.from_config  # the reference constructs SceneDesc from the scene list
@@ -252,6 +279,18 @@ class Renderer:
     def getGammaCorrectionTerm(self):
         return self.launch_params().gammaTerm
 
+    def dumpFramebuffer(self, path=None):
+        """Renderer::dumpFramebuffer: PNG of processImage's RGBA8 (default output.png)."""
+        check(lib.optpt_save_image(self._h, 0, None if path is None else str(path).encode()))
+
+    def dumpAccumFramebufferRgbe(self, path=None):
+        """Renderer::dumpAccumFramebufferRgbe: Radiance .hdr of the mean radiance (default output.hdr)."""
+        check(lib.optpt_save_image(self._h, 1, None if path is None else str(path).encode()))
+
+    def dumpAccumFramebufferExr(self, path=None):
+        """The EXR dump: HALF RGBA of the mean radiance, ZIP (default output.exr)."""
+        check(lib.optpt_save_image(self._h, 2, None if path is None else str(path).encode()))
+
     def getDenoiserState(self):
         return False
 
@@ -282,6 +321,24 @@ class Renderer:
         q = np.empty((lp.h, lp.w, 4), np.float64)
         check(lib.optpt_read_accum(self._h, s.ctypes.data, q.ctypes.data, _stream_handle(stream)))
         return s[..., :3], q[..., :3], self.getSampleCount()
+
+    def rgba8(self, stream=None):
+        """processImage's packed RGBA8 of the tone-mapped frame: (h, w, 4) uint8."""
+        lp = self.launch_params()
+        out = np.empty((lp.h, lp.w), np.uint32)
+        check(lib.optpt_read_rgba8(self._h, out.ctypes.data, _stream_handle(stream)))
+        return out.view(np.uint8).reshape(lp.h, lp.w, 4)
+
+    def image_out(self, rgba8=None, rgbe=None, half_rows=None, stream=None):
+        """The fused output kernel into caller device buffers (torch tensors or None)."""
+        ptr = (lambda t: None if t is None else t.data_ptr())
+        check(lib.optpt_image_out(self._h, ptr(rgba8), ptr(rgbe), ptr(half_rows), _stream_handle(stream)))
+
+    def image_out_profile(self, reps=20):
+        """Milliseconds per output-kernel launch (all payloads, L2 evicted before each)."""
+        ms = ctypes.c_float()
+        check(lib.optpt_image_out_profiled(self._h, reps, ctypes.byref(ms)))
+        return ms.value
 
     def device_buffers(self):
         fb, afb, s, q = (ctypes.c_void_p() for _ in range(4))

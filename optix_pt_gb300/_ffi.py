@@ -165,6 +165,17 @@ _sigs = {
     "optpt_scene_from_gltf": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.POINTER(SceneStruct)]),
     "optpt_image_decode_png": (ctypes.c_int, [_P, ctypes.c_size_t, ctypes.POINTER(Image)]),
     "optpt_image_release": (None, [ctypes.POINTER(Image)]),
+    "optpt_image_out": (ctypes.c_int, [_H, _P, _P, _P, _P]),
+    "optpt_read_rgba8": (ctypes.c_int, [_H, _P, _P]),
+    "optpt_image_out_profiled": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]),
+    "optpt_save_image": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_char_p]),
+    "optpt_encode_png": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_size_t, ctypes.POINTER(_P),
+                                        ctypes.POINTER(ctypes.c_size_t)]),
+    "optpt_encode_hdr": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_P),
+                                        ctypes.POINTER(ctypes.c_size_t)]),
+    "optpt_encode_exr": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(_P),
+                                        ctypes.POINTER(ctypes.c_size_t)]),
+    "optpt_free": (None, [_P]),
     "optpt_create": (ctypes.c_int, [ctypes.POINTER(SceneStruct), ctypes.POINTER(Options), ctypes.POINTER(_H)]),
     "optpt_destroy": (ctypes.c_int, [_H]),
     "optpt_setup_output_buffer": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32]),

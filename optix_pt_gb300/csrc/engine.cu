@@ -2,14 +2,17 @@
 // build, wavefront buffers, the CUDA-graph-captured bounce loop, and the
 // parity entry points. Replaces the reference's Renderer
 // (src/renderer.cpp:24-1762) minus OptiX set-up, denoiser and GL display.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 #include "../../include/optpt.h"
 #include "engine.h"
+#include "image_io.h"
 #include "guide_net.h"
 
 int uploadSrgbTable();
@@ -75,6 +78,8 @@ struct optpt_renderer {
     LaunchShape shape{};
     std::vector<float> hostFb;
     bool hostFbValid = false;
+    void *outScratch = nullptr;  // device payloads of optpt_read_rgba8 / optpt_save_image
+    size_t outScratchBytes = 0;
 
     // graph of one pass, re-captured when the frame parameters change
     cudaGraph_t graph = nullptr;
@@ -251,6 +256,7 @@ struct optpt_renderer {
         cudaFree(dEmisTc);
         cudaFree(dTexels);
         cudaFree(dTexInfo);
+        cudaFree(outScratch);
         if (ownStream)
             cudaStreamDestroy(ownStream);
     }
@@ -1248,6 +1254,141 @@ int optpt_read_frame_buffer(optpt_renderer *r, float *rgbaHost, void *stream)
                                    cudaMemcpyDeviceToHost, st),
                    "frame buffer copy");
     CUDA_OR_RETURN(cudaStreamSynchronize(st), "frame buffer copy");
+    return OPTPT_OK;
+}
+
+int optpt_image_out(optpt_renderer *r, uint32_t *rgba8, uint32_t *rgbe, void *halfRows, void *stream)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    launchImageOut(r->acc.frameBuffer, r->acc.accumFrameBuffer, r->w, r->h, rgba8, rgbe, halfRows,
+                   (cudaStream_t)stream);
+    CUDA_OR_RETURN(cudaGetLastError(), "image output kernel");
+    return OPTPT_OK;
+}
+
+namespace {
+
+int outScratch(optpt_renderer *r, size_t bytes, void **p)
+{
+    if (r->outScratchBytes < bytes) {
+        cudaFree(r->outScratch);
+        r->outScratch = nullptr;
+        r->outScratchBytes = 0;
+        CUDA_OR_RETURN(cudaMalloc(&r->outScratch, bytes), "image output scratch");
+        r->outScratchBytes = bytes;
+    }
+    *p = r->outScratch;
+    return OPTPT_OK;
+}
+
+}  // namespace
+
+int optpt_image_out_profiled(optpt_renderer *r, uint32_t reps, float *msPerLaunch)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (!msPerLaunch || reps == 0)
+        return fail(OPTPT_ERR_INVALID, "NULL output or zero repetitions");
+    const size_t npix = (size_t)r->w * r->h, flushBytes = (size_t)256 << 20;
+    void *d = nullptr, *flush = nullptr;
+    if ((rc = outScratch(r, npix * 16, &d)))
+        return rc;
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "image output profile");
+    CUDA_OR_RETURN(cudaMalloc(&flush, flushBytes), "L2 flush buffer");
+    cudaStream_t st = r->ownStream;
+    uint32_t *rgba8 = (uint32_t *)d, *rgbe = rgba8 + npix;
+    void *rows = rgbe + npix;
+    std::vector<cudaEvent_t> ev(2 * reps, nullptr);
+    cudaError_t e = cudaSuccess;
+    for (auto &x : ev)
+        if (e == cudaSuccess)
+            e = cudaEventCreate(&x);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        launchImageOut(r->acc.frameBuffer, r->acc.accumFrameBuffer, r->w, r->h, rgba8, rgbe, rows, st);
+    // Each launch follows a 256 MB write (L2 is 129 MB): it starts cold.
+    for (uint32_t k = 0; k < reps && e == cudaSuccess; ++k) {
+        cudaMemsetAsync(flush, (int)(k & 0xFF), flushBytes, st);
+        cudaEventRecord(ev[2 * k], st);
+        launchImageOut(r->acc.frameBuffer, r->acc.accumFrameBuffer, r->w, r->h, rgba8, rgbe, rows, st);
+        cudaEventRecord(ev[2 * k + 1], st);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    float total = 0.0f;
+    for (uint32_t k = 0; k < reps && e == cudaSuccess; ++k) {
+        float ms = 0.0f;
+        e = cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]);
+        total += ms;
+    }
+    for (auto &x : ev)
+        if (x)
+            cudaEventDestroy(x);
+    cudaFree(flush);
+    CUDA_OR_RETURN(e, "image output profile");
+    *msPerLaunch = total / (float)reps;
+    return OPTPT_OK;
+}
+
+int optpt_read_rgba8(optpt_renderer *r, uint32_t *rgbaHost, void *stream)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (!rgbaHost)
+        return fail(OPTPT_ERR_INVALID, "NULL destination");
+    void *d = nullptr;
+    const size_t bytes = sizeof(uint32_t) * r->w * r->h;
+    if ((rc = outScratch(r, bytes, &d)))
+        return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    launchImageOut(r->acc.frameBuffer, nullptr, r->w, r->h, (uint32_t *)d, nullptr, nullptr, st);
+    CUDA_OR_RETURN(cudaGetLastError(), "image output kernel");
+    CUDA_OR_RETURN(cudaMemcpyAsync(rgbaHost, d, bytes, cudaMemcpyDeviceToHost, st), "rgba8 copy");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "rgba8 copy");
+    return OPTPT_OK;
+}
+
+int optpt_save_image(optpt_renderer *r, int format, const char *path)
+{
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (format < 0 || format > 2)
+        return fail(OPTPT_ERR_INVALID, "format must be 0 (PNG), 1 (HDR) or 2 (EXR)");
+    static const char *names[3] = {"output.png", "output.hdr", "output.exr"};
+    const size_t npix = (size_t)r->w * r->h;
+    const size_t bytes = format == 2 ? npix * 8 : npix * 4;
+    // The frame may have been rendered on any stream: wait for all of it
+    // (the reference's launch() is synchronous, src/renderer.cpp:949).
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "save image");
+    void *d = nullptr;
+    if ((rc = outScratch(r, bytes, &d)))
+        return rc;
+    cudaStream_t st = r->ownStream;
+    launchImageOut(r->acc.frameBuffer, r->acc.accumFrameBuffer, r->w, r->h, format == 0 ? (uint32_t *)d : nullptr,
+                   format == 1 ? (uint32_t *)d : nullptr, format == 2 ? d : nullptr, st);
+    CUDA_OR_RETURN(cudaGetLastError(), "image output kernel");
+    std::vector<uint8_t> payload(bytes), file;
+    CUDA_OR_RETURN(cudaMemcpyAsync(payload.data(), d, bytes, cudaMemcpyDeviceToHost, st), "image payload copy");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "image payload copy");
+    const int threads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (format == 0)
+        optimg::encodePng(payload.data(), r->w, r->h, (size_t)r->w * 4, file, threads);
+    else if (format == 1)
+        optimg::encodeHdr(payload.data(), r->w, r->h, file);
+    else
+        optimg::encodeExr((const uint16_t *)payload.data(), r->w, r->h, 3, file, threads);
+    const char *name = path ? path : names[format];
+    FILE *f = fopen(name, "wb");
+    if (!f)
+        return fail(OPTPT_ERR_IO, (std::string("cannot open ") + name + " for writing").c_str());
+    const size_t wrote = fwrite(file.data(), 1, file.size(), f);
+    const bool ok = fclose(f) == 0 && wrote == file.size();
+    if (!ok)
+        return fail(OPTPT_ERR_IO, (std::string("cannot write ") + name).c_str());
     return OPTPT_OK;
 }
 

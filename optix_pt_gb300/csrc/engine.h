@@ -204,6 +204,9 @@ void launchGuideInfer(const optpt_guide *g, const DevScene &s, const FrameParams
                       cudaStream_t st);
 void launchGuideGather(const FrameParams &fp, const WaveBufs &q, cudaStream_t st);
 int occupancyGrid(int kernelId, int block);  // persistent grid for a kernel class
+// Frame output payloads (image_out.cu): any output pointer may be null.
+void launchImageOut(const float4 *fb, const float4 *mean, uint32_t w, uint32_t h, uint32_t *rgba8, uint32_t *rgbe,
+                    void *halfRows, cudaStream_t st);
 
 // bvh_build.cu, bvh8_build.cu
 struct Bvh8Node;

@@ -32,4 +32,25 @@ bool isPng(const uint8_t *p, size_t n);
 // high byte, low bit depths scale to 0..255, palette and tRNS apply.
 bool decodePng(const uint8_t *p, size_t n, Image &img, std::string &err);
 
+// ---------------------------------------------------------------- encoders
+// DEFLATE with dynamic Huffman codes (greedy LZ77 over a 32 KB window, hash
+// chains; a block falls back to stored when that is smaller). `sync` ends
+// the stream with an empty stored block instead of a final block, so that
+// independently compressed pieces concatenate into one stream.
+void deflate(const uint8_t *in, size_t n, std::vector<uint8_t> &out, bool sync);
+// zlib stream of `n` bytes split into pieces compressed on up to `threads`
+// host threads (piece boundaries on multiples of `grain` bytes).
+void zlibCompress(const uint8_t *in, size_t n, std::vector<uint8_t> &out, int threads, size_t grain);
+
+// PNG (8-bit RGBA, colour type 6) of rows top to bottom; per-row filter
+// chosen by the minimum sum of absolute residuals.
+void encodePng(const uint8_t *rgba, uint32_t w, uint32_t h, size_t stride, std::vector<uint8_t> &out, int threads);
+// Radiance RGBE (.hdr) from pre-converted RGBE pixels (4 bytes each), with
+// run-length encoded scanlines for widths 8..32767.
+void encodeHdr(const uint8_t *rgbe, uint32_t w, uint32_t h, std::vector<uint8_t> &out);
+// OpenEXR scanline file, channels A, B, G, R as HALF; `rows` holds each
+// scanline channel-planar (A[w], B[w], G[w], R[w] as 16-bit halves), the
+// layout an EXR scanline stores. compression: 0 none, 3 ZIP (16 lines).
+bool encodeExr(const uint16_t *rows, uint32_t w, uint32_t h, int compression, std::vector<uint8_t> &out, int threads);
+
 }  // namespace optimg
