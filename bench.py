@@ -467,6 +467,19 @@ def run_ours(args, rank, world, local_rank):
                 "kernel_share": {k: v / sum(kms.values()) for k, v in kms.items()}}
 
     image_output = image_output_measure(r, peak) if world == 1 else None
+    # Animation: BVH8 refit of this scene (the reference's per-frame
+    # buildAccel(false)), kernel time, against a rebuild measured on the host
+    # clock around the whole LBVH build + collapse.
+    animation = None
+    if world == 1:
+        refit_ms = r.refit_profile(20)
+        t0 = time.perf_counter()
+        r2 = opt.Renderer(scene)
+        rebuild_s = time.perf_counter() - t0
+        r2.close()
+        animation = {"refit_ms": refit_ms, "triangles": scene.num_triangles,
+                     "renderer_create_with_bvh_build_ms": rebuild_s * 1e3,
+                     "refit_mtris_per_s": scene.num_triangles / (refit_ms / 1e3) / 1e6}
 
     guided = None
     if world == 1 and not args.no_guided:
@@ -493,7 +506,7 @@ def run_ours(args, rank, world, local_rank):
                     "d2h_bytes_per_step": w * h * 16},
             "gpu_launches": passes_launches * args.steps,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "guided_vs_plain_equal_time": guided, "image_output": image_output}
+            "guided_vs_plain_equal_time": guided, "image_output": image_output, "animation": animation}
     print(json.dumps(line))
     r.close()
 

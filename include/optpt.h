@@ -117,6 +117,57 @@ int optpt_scene_from_config(const char *sceneListPath, optpt_scene *out);
  * unreadable file, OPTPT_ERR_PARSE for malformed JSON, buffers or images. */
 int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *out);
 
+/* ------------------------------------------------------------------ animation */
+
+/* A glTF scene kept in memory so that it can be posed at any time: its node
+ * tree, skins and one animation (the reference's loadAnimations,
+ * src/gltf_loader.cpp:1390-1509: animation 2 when the file has three or
+ * more, else 0), evaluated as Renderer::updateScene does each frame
+ * (src/renderer.cpp:1060-1303). */
+typedef struct optpt_gltf optpt_gltf;
+
+typedef struct optpt_gltf_info_t {
+    uint32_t numVertices;   /* of the flattened scene                      */
+    uint32_t numShapes;     /* mesh nodes (one matrix slot each)           */
+    uint32_t numJointSlots; /* joint matrices over all skinned shapes      */
+    uint32_t numChannels;   /* animated translation/rotation/scale targets */
+    float duration;         /* last key time of the animation (0: static)  */
+    int32_t skinned;
+} optpt_gltf_info_t;
+
+/* How each vertex of a renderer's scene follows a pose: rest position (and
+ * normal) in its shape's space, the shape's matrix slot and, for skinned
+ * vertices, four joint-matrix slots and weights (joints/weights NULL when
+ * nothing is skinned). Host arrays. */
+typedef struct optpt_deformation {
+    const float *restPositions; /* float3 per vertex                        */
+    const float *restNormals;   /* float3 per vertex, or NULL               */
+    const uint32_t *vertexShape;
+    const uint16_t *joints;     /* 4 per vertex, or NULL                    */
+    const float *weights;       /* 4 per vertex, or NULL                    */
+    uint32_t numVertices;
+    uint32_t numShapes;
+    uint32_t numJoints;
+} optpt_deformation;
+
+int optpt_gltf_open(const char *path, const float upHint[3], optpt_gltf **out);
+void optpt_gltf_close(optpt_gltf *g);
+int optpt_gltf_info(const optpt_gltf *g, optpt_gltf_info_t *info);
+/* The flattened scene at `time` (animate 0: rest pose, no animation), into
+ * library-owned arrays released with optpt_scene_release. */
+int optpt_gltf_scene(const optpt_gltf *g, float time, int animate, optpt_scene *out);
+/* Pointers into the model (valid until optpt_gltf_close). */
+int optpt_gltf_deformation(const optpt_gltf *g, optpt_deformation *out);
+/* The pose at `time`: per shape its world matrix (16 floats, column-major)
+ * and normal matrix (9 floats, row r multiplies the normal: the inverse
+ * transpose of the world matrix's 3x3); per joint slot inverse(world(mesh
+ * node)) * world(joint) * inverseBind. Any output may be NULL. */
+int optpt_gltf_pose(const optpt_gltf *g, float time, float *shapeMatrices, float *shapeNormalMatrices,
+                    float *jointMatrices);
+/* Positions (and normals, if the scene has them) of every vertex at `time`,
+ * on the host, with the same float operations as optpt_deform. */
+int optpt_gltf_apply(const optpt_gltf *g, float time, float *positions, float *normals);
+
 /* An RGBA8 image in library-owned memory. */
 typedef struct optpt_image {
     uint32_t width;
@@ -201,6 +252,38 @@ int optpt_read_frame_buffer(optpt_renderer *r, float *rgbaHost, void *stream);
 /* Copies the FP64 per-pixel sums (double4 sum and sum of squares, xyz used,
  * w*h each) to caller host memory, ordered on `stream`, and waits for it. */
 int optpt_read_accum(optpt_renderer *r, double *sumHost, double *sumSqHost, void *stream);
+
+/* ------------------------------------------------------------------ scene updates */
+
+/* New vertex positions (and normals, if the scene has them; either may be
+ * NULL) as host arrays of the scene's vertex count, then the per-frame work
+ * of Renderer::updateScene + updateAccel (src/renderer.cpp:1060-1303): the
+ * acceleration structure is refit on the GPU (BVH8: triangle records
+ * regathered and every level's quantised boxes recomputed bottom-up, topology
+ * kept, as OptiX's update keeps it; the binary BVH is rebuilt), the emissive
+ * triangles follow, and accumulation restarts (resetSampleCount). Ordered on
+ * `stream`; returns without waiting. */
+int optpt_update_vertices(optpt_renderer *r, const float *positions, const float *normals, void *stream);
+
+/* Uploads how the scene's vertices follow a pose (see optpt_deformation and
+ * optpt_gltf_deformation); once, before optpt_deform. */
+int optpt_set_deformation(optpt_renderer *r, const optpt_deformation *d);
+
+/* Poses the scene on the GPU: uploads the shape matrices (16 floats each),
+ * shape normal matrices (9 each) and joint matrices (16 each; NULL when
+ * nothing is skinned), deforms every vertex in a kernel with the float
+ * operations of optpt_gltf_apply (bit-identical results), then refits as
+ * optpt_update_vertices does. Ordered on `stream`. */
+int optpt_deform(optpt_renderer *r, const float *shapeMatrices, const float *shapeNormalMatrices,
+                 const float *jointMatrices, void *stream);
+
+/* Average CUDA-event time of `reps` back-to-back BVH8 refits of the
+ * current vertices (triangle records + every level), for measurement. */
+int optpt_refit_profiled(optpt_renderer *r, uint32_t reps, float *msPerRefit);
+
+/* Copies the current vertex positions / normals (either may be NULL) to
+ * host memory, ordered on `stream`; waits for it. */
+int optpt_read_vertices(optpt_renderer *r, float *positions, float *normals, void *stream);
 
 /* ------------------------------------------------------------------ image output */
 

@@ -15,7 +15,7 @@ import numpy as np
 from . import _ffi
 from ._ffi import BSDF_QUERY, BSDF_RESULT, OptptError, check, lib
 
-__all__ = ["Scene", "SceneDesc", "decode_png", "encode_png", "encode_hdr", "encode_exr", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
+__all__ = ["Scene", "SceneDesc", "GltfModel", "Animator", "decode_png", "encode_png", "encode_hdr", "encode_exr", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
            "library_path"]
 
 library_path = _ffi.LIB_PATH
@@ -123,6 +123,76 @@ def decode_png(data):
             img.height, img.width, 4)
     finally:
         lib.optpt_image_release(ctypes.byref(img))
+
+
+class GltfModel:
+    """A glTF scene kept for posing (node tree, skins, one animation): the
+    reference's GltfLoader + the animation half of Renderer::updateScene."""
+
+    def __init__(self, path, up=(0.0, 1.0, 0.0)):
+        self._h = None
+        h = ctypes.c_void_p()
+        u = (ctypes.c_float * 3)(*up)
+        check(lib.optpt_gltf_open(str(path).encode(), ctypes.cast(u, ctypes.c_void_p), ctypes.byref(h)))
+        self._h = h.value
+        inf = _ffi.GltfInfo()
+        check(lib.optpt_gltf_info(self._h, ctypes.byref(inf)))
+        self.info = {k: getattr(inf, k) for k, _ in _ffi.GltfInfo._fields_}
+
+    def close(self):
+        if self._h:
+            lib.optpt_gltf_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def scene(self, time=0.0, animate=False):
+        s = _ffi.SceneStruct()
+        check(lib.optpt_gltf_scene(self._h, time, 1 if animate else 0, ctypes.byref(s)))
+        return Scene(s, True)
+
+    def deformation(self):
+        d = _ffi.Deformation()
+        check(lib.optpt_gltf_deformation(self._h, ctypes.byref(d)))
+        return d
+
+    def pose(self, time):
+        """(shape matrices (S, 16), shape normal matrices (S, 9), joint matrices (J, 16)) at `time`."""
+        S, J = self.info["numShapes"], self.info["numJointSlots"]
+        m = np.zeros((S, 16), np.float32)
+        n = np.zeros((S, 9), np.float32)
+        j = np.zeros((max(J, 1), 16), np.float32)
+        check(lib.optpt_gltf_pose(self._h, time, m.ctypes.data, n.ctypes.data, j.ctypes.data))
+        return m, n, j[:J]
+
+    def apply(self, time):
+        """Positions (and normals) of every vertex at `time`, evaluated on the host."""
+        nv = self.info["numVertices"]
+        p = np.zeros((nv, 3), np.float32)
+        n = np.zeros((nv, 3), np.float32)
+        check(lib.optpt_gltf_apply(self._h, time, p.ctypes.data, n.ctypes.data))
+        return p, n
+
+
+class Animator:
+    """Drives a renderer from a GltfModel as the reference's per-frame
+    updateScene does: the clock advances 0.02 per frame, the pose is
+    evaluated on the host (a few matrices) and the vertices are deformed and
+    the BVH refit on the GPU."""
+
+    def __init__(self, renderer, model, dt=0.02):
+        self.r, self.model, self.dt, self.t = renderer, model, dt, 0.0
+        check(lib.optpt_set_deformation(renderer._h, ctypes.byref(model.deformation())))
+
+    def pose(self, time, stream=None):
+        self.t = time
+        m, n, j = self.model.pose(time)
+        check(lib.optpt_deform(self.r._h, m.ctypes.data, n.ctypes.data, j.ctypes.data if len(j) else None,
+                               _stream_handle(stream)))
+
+    def step(self, stream=None):
+        self.pose(self.t + self.dt, stream)
 
 
 def _encoded(fn, *args):
@@ -333,6 +403,26 @@ class Renderer:
         """The fused output kernel into caller device buffers (torch tensors or None)."""
         ptr = (lambda t: None if t is None else t.data_ptr())
         check(lib.optpt_image_out(self._h, ptr(rgba8), ptr(rgbe), ptr(half_rows), _stream_handle(stream)))
+
+    def update_vertices(self, positions, normals=None, stream=None):
+        p = np.ascontiguousarray(positions, np.float32)
+        n = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        # pageable host memory: the copy has consumed the arrays when the call returns
+        check(lib.optpt_update_vertices(self._h, p.ctypes.data, None if n is None else n.ctypes.data,
+                                        _stream_handle(stream)))
+
+    def read_vertices(self, stream=None):
+        nv = self.scene.struct.numVertices
+        p = np.empty((nv, 3), np.float32)
+        n = np.empty((nv, 3), np.float32)
+        check(lib.optpt_read_vertices(self._h, p.ctypes.data, n.ctypes.data, _stream_handle(stream)))
+        return p, n
+
+    def refit_profile(self, reps=20):
+        """Milliseconds per BVH8 refit of the current vertices."""
+        ms = ctypes.c_float()
+        check(lib.optpt_refit_profiled(self._h, reps, ctypes.byref(ms)))
+        return ms.value
 
     def image_out_profile(self, reps=20):
         """Milliseconds per output-kernel launch (all payloads, L2 evicted before each)."""

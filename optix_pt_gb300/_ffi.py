@@ -86,6 +86,17 @@ class Image(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("rgba", ctypes.POINTER(ctypes.c_uint8))]
 
 
+class GltfInfo(ctypes.Structure):
+    _fields_ = [("numVertices", ctypes.c_uint32), ("numShapes", ctypes.c_uint32), ("numJointSlots", ctypes.c_uint32),
+                ("numChannels", ctypes.c_uint32), ("duration", ctypes.c_float), ("skinned", ctypes.c_int32)]
+
+
+class Deformation(ctypes.Structure):
+    _fields_ = [("restPositions", ctypes.c_void_p), ("restNormals", ctypes.c_void_p),
+                ("vertexShape", ctypes.c_void_p), ("joints", ctypes.c_void_p), ("weights", ctypes.c_void_p),
+                ("numVertices", ctypes.c_uint32), ("numShapes", ctypes.c_uint32), ("numJoints", ctypes.c_uint32)]
+
+
 class SceneStruct(ctypes.Structure):
     _fields_ = [("positions", ctypes.POINTER(ctypes.c_float)), ("numVertices", ctypes.c_uint32),
                 ("normals", ctypes.POINTER(ctypes.c_float)), ("texCoords", ctypes.POINTER(ctypes.c_float)),
@@ -165,6 +176,18 @@ _sigs = {
     "optpt_scene_from_gltf": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.POINTER(SceneStruct)]),
     "optpt_image_decode_png": (ctypes.c_int, [_P, ctypes.c_size_t, ctypes.POINTER(Image)]),
     "optpt_image_release": (None, [ctypes.POINTER(Image)]),
+    "optpt_gltf_open": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.POINTER(_P)]),
+    "optpt_gltf_close": (None, [_P]),
+    "optpt_gltf_info": (ctypes.c_int, [_P, ctypes.POINTER(GltfInfo)]),
+    "optpt_gltf_scene": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int, ctypes.POINTER(SceneStruct)]),
+    "optpt_gltf_deformation": (ctypes.c_int, [_P, ctypes.POINTER(Deformation)]),
+    "optpt_gltf_pose": (ctypes.c_int, [_P, ctypes.c_float, _P, _P, _P]),
+    "optpt_gltf_apply": (ctypes.c_int, [_P, ctypes.c_float, _P, _P]),
+    "optpt_update_vertices": (ctypes.c_int, [_H, _P, _P, _P]),
+    "optpt_set_deformation": (ctypes.c_int, [_H, ctypes.POINTER(Deformation)]),
+    "optpt_deform": (ctypes.c_int, [_H, _P, _P, _P, _P]),
+    "optpt_read_vertices": (ctypes.c_int, [_H, _P, _P, _P]),
+    "optpt_refit_profiled": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]),
     "optpt_image_out": (ctypes.c_int, [_H, _P, _P, _P, _P]),
     "optpt_read_rgba8": (ctypes.c_int, [_H, _P, _P]),
     "optpt_image_out_profiled": (ctypes.c_int, [_H, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]),

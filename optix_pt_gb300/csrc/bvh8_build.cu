@@ -213,7 +213,134 @@ __global__ void kCollapseEmit(const int *__restrict__ items, int nItems, const E
     out[levelStart + i] = N;
 }
 
+// Refit, step 1: the leaf-ordered triangle records take the new vertex
+// positions (the record's w fields, prim id, material and flags, are kept).
+__global__ void kRefitTris(int n, const float *__restrict__ pos, const int *__restrict__ idx,
+                           float4 *__restrict__ triV8)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    float4 *t = triV8 + 3 * (size_t)k;
+    const int prim = __float_as_int(t[0].w);
+    if (prim < 0 || prim >= n)
+        return;
+    for (int v = 0; v < 3; ++v) {
+        const int vi = __ldg(idx + 3 * prim + v);
+        float4 r = t[v];
+        r.x = __ldg(pos + 3 * (size_t)vi);
+        r.y = __ldg(pos + 3 * (size_t)vi + 1);
+        r.z = __ldg(pos + 3 * (size_t)vi + 2);
+        t[v] = r;
+    }
+}
+
+// Refit, step 2 (one launch per level, deepest first): each node's child
+// boxes from its internal children's refit boxes and its leaf triangles,
+// its frame and quantised boxes recomputed exactly as kCollapseEmit does.
+// With unchanged vertices the nodes come out bit-identical.
+__global__ void kRefitLevel(int begin, int end, Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV8,
+                            float *__restrict__ box8, int numNodes8, int numTris)
+{
+    const int i = begin + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= end)
+        return;
+    Bvh8Node N = nodes[i];
+    const uint32_t ew = __float_as_uint(N.a.w), imask = ew >> 24;
+    const float inf = __int_as_float(0x7f800000);
+    float elo[8][3], ehi[8][3];
+    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+    uint32_t present = 0;
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t meta = byteOf(N.b, 8 + s);
+        for (int k = 0; k < 3; ++k) {
+            elo[s][k] = inf;
+            ehi[s][k] = -inf;
+        }
+        if (meta == 0u)
+            continue;
+        present |= 1u << s;
+        if ((imask >> s) & 1u) {
+            const int c = (int)N.b.x + __popc(imask & ((1u << s) - 1u));
+            if (c < 0 || c >= numNodes8)
+                continue;
+            for (int k = 0; k < 3; ++k) {
+                elo[s][k] = box8[6 * (size_t)c + k];
+                ehi[s][k] = box8[6 * (size_t)c + 3 + k];
+            }
+        } else {
+            const int first = (int)N.b.y + (int)(meta & 31u), cnt = (int)(meta >> 5);
+            for (int t = first; t < first + cnt && t < numTris; ++t)
+                for (int v = 0; v < 3; ++v) {
+                    const float4 p = triV8[3 * (size_t)t + v];
+                    elo[s][0] = fminf(elo[s][0], p.x);
+                    elo[s][1] = fminf(elo[s][1], p.y);
+                    elo[s][2] = fminf(elo[s][2], p.z);
+                    ehi[s][0] = fmaxf(ehi[s][0], p.x);
+                    ehi[s][1] = fmaxf(ehi[s][1], p.y);
+                    ehi[s][2] = fmaxf(ehi[s][2], p.z);
+                }
+        }
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], elo[s][k]);
+            hi[k] = fmaxf(hi[k], ehi[s][k]);
+        }
+    }
+    int ex[3];
+    for (int k = 0; k < 3; ++k)
+        ex[k] = scaleExponent((double)hi[k] - (double)lo[k]);
+    uint32_t qlo[3][8], qhi[3][8];
+    for (int s = 0; s < 8; ++s) {
+        for (int k = 0; k < 3; ++k) {
+            qlo[k][s] = qhi[k][s] = 0u;
+            if (!((present >> s) & 1u))
+                continue;
+            const double inv = ldexp(1.0, -ex[k]);
+            double ql = floor(((double)elo[s][k] - (double)lo[k]) * inv);
+            double qh = ceil(((double)ehi[s][k] - (double)lo[k]) * inv);
+            ql = ql > 0.0 ? ql - 1.0 : 0.0;
+            qh = fmin(qh + 1.0, 255.0);
+            qlo[k][s] = (uint32_t)ql;
+            qhi[k][s] = (uint32_t)qh;
+        }
+    }
+    const uint32_t nw = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) | ((uint32_t)(ex[2] + 127) << 16) |
+                        (imask << 24);
+    N.a = make_float4(lo[0], lo[1], lo[2], __uint_as_float(nw));
+    uint4 *q[3] = {&N.qx, &N.qy, &N.qz};
+    for (int k = 0; k < 3; ++k) {
+        q[k]->x = qlo[k][0] | qlo[k][1] << 8 | qlo[k][2] << 16 | qlo[k][3] << 24;
+        q[k]->y = qlo[k][4] | qlo[k][5] << 8 | qlo[k][6] << 16 | qlo[k][7] << 24;
+        q[k]->z = qhi[k][0] | qhi[k][1] << 8 | qhi[k][2] << 16 | qhi[k][3] << 24;
+        q[k]->w = qhi[k][4] | qhi[k][5] << 8 | qhi[k][6] << 16 | qhi[k][7] << 24;
+    }
+    nodes[i] = N;
+    for (int k = 0; k < 3; ++k) {
+        box8[6 * (size_t)i + k] = lo[k];
+        box8[6 * (size_t)i + 3 + k] = hi[k];
+    }
+}
+
 }  // namespace
+
+int refitBvh8(BvhBuild &b, const float *positions, const int *triIndices, int numTris, cudaStream_t st)
+{
+    if (numTris <= 0 || b.nodes8 == nullptr)
+        return 0;
+    if (!b.box8) {
+        cudaError_t e = cudaMalloc(&b.box8, sizeof(float) * 6 * (size_t)(b.numNodes8 > 0 ? b.numNodes8 : 1));
+        if (e != cudaSuccess)
+            return (int)e;
+    }
+    kRefitTris<<<(numTris + 255) / 256, 256, 0, st>>>(numTris, positions, triIndices, b.triV8);
+    for (int l = b.levels8 - 1; l >= 0; --l) {
+        const int begin = b.levelOff8[l], end = b.levelOff8[l + 1];
+        if (end > begin)
+            kRefitLevel<<<(end - begin + 127) / 128, 128, 0, st>>>(begin, end, b.nodes8, b.triV8, b.box8,
+                                                                  b.numNodes8, numTris);
+    }
+    return (int)cudaGetLastError();
+}
 
 // Collapses a built BVH2 (`in`) into in.nodes8 / in.triV8. Returns 0 or a CUDA
 // error code.
@@ -249,6 +376,7 @@ int buildBvh8(BvhBuild &in, int numTris, cudaStream_t st)
     CK8(cudaMalloc(&temp, tempBytes));
     CK8(cudaMemcpyAsync(items, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     while (nItems > 0 && levels < 256) {
+        in.levelOff8[levels] = levelStart;
         const int G = (nItems + 127) / 128;
         kCollapseOpen<<<G, 128, 0, st>>>(in.nodes, items, nItems, ent, nEnt, kInt, nTri);
         // one extra zero entry so the exclusive scan's last element is the total
@@ -279,6 +407,7 @@ int buildBvh8(BvhBuild &in, int numTris, cudaStream_t st)
     }
     in.numNodes8 = levelStart;
     in.levels8 = levels;
+    in.levelOff8[levels] = levelStart;
     if (triStart != numTris)
         err = cudaErrorInvalidValue;
 done:

@@ -393,5 +393,6 @@ void freeBvh(BvhBuild &b)
     cudaFree(b.primOrder);
     cudaFree(b.nodes8);
     cudaFree(b.triV8);
+    cudaFree(b.box8);
     b = BvhBuild{};
 }

@@ -81,6 +81,15 @@ struct optpt_renderer {
     void *outScratch = nullptr;  // device payloads of optpt_read_rgba8 / optpt_save_image
     size_t outScratchBytes = 0;
 
+    // deformation (optpt_set_deformation / optpt_deform / optpt_update_vertices)
+    uint32_t numVerts = 0;
+    int *dEmisPrim = nullptr;
+    float *dRestPos = nullptr, *dRestNrm = nullptr, *dShapeM = nullptr, *dShapeN = nullptr, *dJointM = nullptr;
+    uint32_t *dVShape = nullptr;
+    void *dJoints = nullptr, *dWeights = nullptr;
+    uint32_t defVerts = 0, defShapes = 0, defJoints = 0;
+    bool hasNormals = false;
+
     // graph of one pass, re-captured when the frame parameters change
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
@@ -257,6 +266,15 @@ struct optpt_renderer {
         cudaFree(dTexels);
         cudaFree(dTexInfo);
         cudaFree(outScratch);
+        cudaFree(dEmisPrim);
+        cudaFree(dRestPos);
+        cudaFree(dRestNrm);
+        cudaFree(dShapeM);
+        cudaFree(dShapeN);
+        cudaFree(dJointM);
+        cudaFree(dVShape);
+        cudaFree(dJoints);
+        cudaFree(dWeights);
         if (ownStream)
             cudaStreamDestroy(ownStream);
     }
@@ -557,6 +575,61 @@ int checkRenderable(optpt_renderer *r)
 
 }  // namespace
 
+namespace {
+
+// After the vertex positions changed (device arrays already updated on
+// `st`): refit (BVH8) or rebuild (BVH2) the acceleration structure,
+// regather the emissive-triangle vertices and restart accumulation, as
+// Renderer::updateAccel does (buildAccel(false) then resetSampleCount,
+// src/renderer.cpp:1299-1303).
+int afterVertexChange(optpt_renderer *r, cudaStream_t st)
+{
+    const int nt = r->scene.numTris;
+    if (r->bvh.nodes8) {
+        int e = refitBvh8(r->bvh, r->dPositions, r->dTriIndices, nt, st);
+        if (e)
+            return cudaFail((cudaError_t)e, "BVH8 refit");
+    } else if (nt > 0) {
+        CUDA_OR_RETURN(cudaStreamSynchronize(st), "BVH rebuild");
+        BvhBuild fresh{};
+        int e = buildBvh(r->dPositions, r->dTriIndices, r->dMatIndices, r->dTriFlags, nt, (int)r->opt.leafSize, fresh,
+                         st);
+        if (e)
+            return cudaFail((cudaError_t)e, "BVH rebuild");
+        freeBvh(r->bvh);
+        r->bvh = fresh;
+        r->scene.nodes = r->bvh.nodes;
+        r->scene.triV = r->bvh.triV;
+        r->scene.numNodes = r->bvh.usedNodes;
+        r->graphDirty = true;          // the captured pass holds the old pointers
+        r->batch.guideMode = -1;
+    }
+    launchEmissiveVerts(r->numEmissive, r->dEmisPrim, r->dPositions, r->dTriIndices, nt, r->dEmisV, st);
+    CUDA_OR_RETURN(cudaGetLastError(), "emissive vertices");
+    if (r->w && r->h) {
+        const size_t npix = (size_t)r->w * r->h;
+        CUDA_OR_RETURN(cudaMemsetAsync(r->acc.sum, 0, sizeof(Acc4) * npix, st), "reset");
+        CUDA_OR_RETURN(cudaMemsetAsync(r->acc.sumSq, 0, sizeof(Acc4) * npix, st), "reset");
+        CUDA_OR_RETURN(cudaMemsetAsync(r->dState, 0, sizeof(uint32_t), st), "reset");
+    }
+    r->lp.sample = 0;
+    r->hostFbValid = false;
+    return OPTPT_OK;
+}
+
+template <class T> int replaceDevice(T *&dst, const T *src, size_t count, const char *what)
+{
+    cudaFree(dst);
+    dst = nullptr;
+    if (!src || !count)
+        return OPTPT_OK;
+    CUDA_OR_RETURN(cudaMalloc((void **)&dst, sizeof(T) * count), what);
+    CUDA_OR_RETURN(cudaMemcpy(dst, src, sizeof(T) * count, cudaMemcpyHostToDevice), what);
+    return OPTPT_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *optpt_last_error(void) { return g_lastError.c_str(); }
@@ -639,10 +712,12 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         // src/renderer.cpp:210-237): emission > 0 or an emissive texture.
         std::vector<float4> emisV, emisRad;
         std::vector<float2> emisTc;
+        std::vector<int> emisPrim;
         for (uint32_t t = 0; t < nt; ++t) {
             const MaterialData &m = s->materials[s->matIndices[t]];
             if (!(m.emission[0] > 0.0f || m.emission[1] > 0.0f || m.emission[2] > 0.0f || m.hasEmissiveTexture))
                 continue;
+            emisPrim.push_back((int)t);
             for (int k = 0; k < 3; ++k) {
                 const int v = s->triIndices[3 * t + k];
                 emisV.push_back(make_float4(s->positions[3 * v], s->positions[3 * v + 1], s->positions[3 * v + 2], 0.0f));
@@ -656,6 +731,8 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         }
         r->numEmissive = (int)emisRad.size();
         r->numLights = (int)s->numLights;
+        r->numVerts = s->numVertices;
+        r->hasNormals = s->normals != nullptr;
         std::vector<uint32_t> texels;
         std::vector<int4> texInfo;
         for (uint32_t t = 0; t < s->numTextures; ++t) {
@@ -680,6 +757,7 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
             (e = upload(r->dEmisV, emisV.data(), emisV.size())) ||
             (e = upload(r->dEmisTc, emisTc.data(), emisTc.size())) ||
             (e = upload(r->dEmisRad, emisRad.data(), emisRad.size())) ||
+            (e = upload(r->dEmisPrim, emisPrim.data(), emisPrim.size())) ||
             (e = upload(r->dTexels, texels.data(), texels.size())) ||
             (e = upload(r->dTexInfo, texInfo.data(), texInfo.size()))) {
             rc = cudaFail(e, "scene upload");
@@ -1254,6 +1332,149 @@ int optpt_read_frame_buffer(optpt_renderer *r, float *rgbaHost, void *stream)
                                    cudaMemcpyDeviceToHost, st),
                    "frame buffer copy");
     CUDA_OR_RETURN(cudaStreamSynchronize(st), "frame buffer copy");
+    return OPTPT_OK;
+}
+
+int optpt_update_vertices(optpt_renderer *r, const float *positions, const float *normals, void *stream)
+{
+    if (!r || !positions)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->dPositions, positions, sizeof(float) * 3 * r->numVerts,
+                                   cudaMemcpyHostToDevice, st),
+                   "vertex upload");
+    if (normals && r->hasNormals)
+        CUDA_OR_RETURN(cudaMemcpyAsync(r->dNormals, normals, sizeof(float) * 3 * r->numVerts,
+                                       cudaMemcpyHostToDevice, st),
+                       "normal upload");
+    return afterVertexChange(r, st);
+}
+
+int optpt_set_deformation(optpt_renderer *r, const optpt_deformation *d)
+{
+    if (!r || !d || !d->restPositions || !d->vertexShape)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if (d->numVertices != r->numVerts)
+        return fail(OPTPT_ERR_INVALID, "deformation vertex count differs from the scene's");
+    if (d->numShapes == 0 || (d->joints && (!d->weights || d->numJoints == 0)))
+        return fail(OPTPT_ERR_INVALID, "deformation needs shapes, and weights and joints together");
+    for (uint32_t v = 0; v < d->numVertices; ++v) {
+        if (d->vertexShape[v] >= d->numShapes)
+            return fail(OPTPT_ERR_INVALID, "vertex shape slot out of range");
+        if (d->joints)
+            for (int k = 0; k < 4; ++k)
+                if (d->weights[4 * v + k] != 0.0f && d->joints[4 * v + k] >= d->numJoints)
+                    return fail(OPTPT_ERR_INVALID, "joint slot out of range");
+    }
+    const size_t nv = d->numVertices;
+    int rc;
+    if ((rc = replaceDevice(r->dRestPos, d->restPositions, 3 * nv, "deformation upload")) ||
+        (rc = replaceDevice(r->dRestNrm, r->hasNormals ? d->restNormals : nullptr, 3 * nv, "deformation upload")) ||
+        (rc = replaceDevice(r->dVShape, d->vertexShape, nv, "deformation upload")))
+        return rc;
+    // Joints with zero weight may hold anything; the kernel checks slots, so
+    // store zero joints where the weight is zero.
+    std::vector<uint16_t> joints;
+    if (d->joints) {
+        joints.assign(d->joints, d->joints + 4 * nv);
+        for (size_t k = 0; k < 4 * nv; ++k)
+            if (d->weights[k] == 0.0f)
+                joints[k] = 0;
+    }
+    cudaFree(r->dJoints);
+    cudaFree(r->dWeights);
+    r->dJoints = r->dWeights = nullptr;
+    if (d->joints) {
+        CUDA_OR_RETURN(cudaMalloc(&r->dJoints, sizeof(uint16_t) * 4 * nv), "deformation upload");
+        CUDA_OR_RETURN(cudaMemcpy(r->dJoints, joints.data(), sizeof(uint16_t) * 4 * nv, cudaMemcpyHostToDevice),
+                       "deformation upload");
+        CUDA_OR_RETURN(cudaMalloc(&r->dWeights, sizeof(float) * 4 * nv), "deformation upload");
+        CUDA_OR_RETURN(cudaMemcpy(r->dWeights, d->weights, sizeof(float) * 4 * nv, cudaMemcpyHostToDevice),
+                       "deformation upload");
+    }
+    cudaFree(r->dShapeM);
+    cudaFree(r->dShapeN);
+    cudaFree(r->dJointM);
+    r->dShapeM = r->dShapeN = r->dJointM = nullptr;
+    CUDA_OR_RETURN(cudaMalloc((void **)&r->dShapeM, sizeof(float) * 16 * d->numShapes), "deformation upload");
+    CUDA_OR_RETURN(cudaMalloc((void **)&r->dShapeN, sizeof(float) * 9 * d->numShapes), "deformation upload");
+    if (d->numJoints)
+        CUDA_OR_RETURN(cudaMalloc((void **)&r->dJointM, sizeof(float) * 16 * d->numJoints), "deformation upload");
+    r->defVerts = d->numVertices;
+    r->defShapes = d->numShapes;
+    r->defJoints = d->joints ? d->numJoints : 0;
+    return OPTPT_OK;
+}
+
+int optpt_deform(optpt_renderer *r, const float *shapeMatrices, const float *shapeNormalMatrices,
+                 const float *jointMatrices, void *stream)
+{
+    if (!r || !shapeMatrices || !shapeNormalMatrices)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    if (!r->defVerts)
+        return fail(OPTPT_ERR_STATE, "no deformation set (call optpt_set_deformation)");
+    if (r->defJoints && !jointMatrices)
+        return fail(OPTPT_ERR_INVALID, "joint matrices required for a skinned deformation");
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->dShapeM, shapeMatrices, sizeof(float) * 16 * r->defShapes,
+                                   cudaMemcpyHostToDevice, st),
+                   "pose upload");
+    CUDA_OR_RETURN(cudaMemcpyAsync(r->dShapeN, shapeNormalMatrices, sizeof(float) * 9 * r->defShapes,
+                                   cudaMemcpyHostToDevice, st),
+                   "pose upload");
+    if (r->defJoints)
+        CUDA_OR_RETURN(cudaMemcpyAsync(r->dJointM, jointMatrices, sizeof(float) * 16 * r->defJoints,
+                                       cudaMemcpyHostToDevice, st),
+                       "pose upload");
+    launchDeform(r->defVerts, r->dRestPos, r->dRestNrm, r->dVShape, r->dJoints, r->dWeights, r->dShapeM, r->dShapeN,
+                 r->dJointM, r->defShapes, r->defJoints, r->dPositions, r->hasNormals ? r->dNormals : nullptr, st);
+    CUDA_OR_RETURN(cudaGetLastError(), "deform kernel");
+    return afterVertexChange(r, st);
+}
+
+int optpt_refit_profiled(optpt_renderer *r, uint32_t reps, float *msPerRefit)
+{
+    if (!r || !msPerRefit || reps == 0)
+        return fail(OPTPT_ERR_INVALID, "NULL argument or zero repetitions");
+    if (!r->bvh.nodes8)
+        return fail(OPTPT_ERR_STATE, "refit timing needs the 8-wide BVH");
+    cudaStream_t st = r->ownStream;
+    CUDA_OR_RETURN(cudaDeviceSynchronize(), "refit profile");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_OR_RETURN(cudaEventCreate(&e0), "refit profile");
+    CUDA_OR_RETURN(cudaEventCreate(&e1), "refit profile");
+    int err = refitBvh8(r->bvh, r->dPositions, r->dTriIndices, r->scene.numTris, st);  // warm (allocates boxes)
+    cudaEventRecord(e0, st);
+    for (uint32_t k = 0; k < reps && !err; ++k)
+        err = refitBvh8(r->bvh, r->dPositions, r->dTriIndices, r->scene.numTris, st);
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess)
+        e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err)
+        return cudaFail((cudaError_t)err, "refit profile");
+    CUDA_OR_RETURN(e, "refit profile");
+    *msPerRefit = ms / (float)reps;
+    return OPTPT_OK;
+}
+
+int optpt_read_vertices(optpt_renderer *r, float *positions, float *normals, void *stream)
+{
+    if (!r)
+        return fail(OPTPT_ERR_INVALID, "NULL renderer");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (positions)
+        CUDA_OR_RETURN(cudaMemcpyAsync(positions, r->dPositions, sizeof(float) * 3 * r->numVerts,
+                                       cudaMemcpyDeviceToHost, st),
+                       "vertex read");
+    if (normals && r->hasNormals)
+        CUDA_OR_RETURN(cudaMemcpyAsync(normals, r->dNormals, sizeof(float) * 3 * r->numVerts,
+                                       cudaMemcpyDeviceToHost, st),
+                       "vertex read");
+    CUDA_OR_RETURN(cudaStreamSynchronize(st), "vertex read");
     return OPTPT_OK;
 }
 

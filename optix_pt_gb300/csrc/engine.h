@@ -204,6 +204,12 @@ void launchGuideInfer(const optpt_guide *g, const DevScene &s, const FrameParams
                       cudaStream_t st);
 void launchGuideGather(const FrameParams &fp, const WaveBufs &q, cudaStream_t st);
 int occupancyGrid(int kernelId, int block);  // persistent grid for a kernel class
+// Vertex deformation and emissive-vertex regather (deform.cu).
+void launchDeform(uint32_t nv, const float *restP, const float *restN, const uint32_t *vShape, const void *joints,
+                  const void *weights, const float *shapeM, const float *shapeN, const float *jointM,
+                  uint32_t numShapes, uint32_t numJoints, float *outP, float *outN, cudaStream_t st);
+void launchEmissiveVerts(int numEmis, const int *emisPrim, const float *pos, const int *idx, int numTris,
+                         float4 *emisV, cudaStream_t st);
 // Frame output payloads (image_out.cu): any output pointer may be null.
 void launchImageOut(const float4 *fb, const float4 *mean, uint32_t w, uint32_t h, uint32_t *rgba8, uint32_t *rgbe,
                     void *halfRows, cudaStream_t st);
@@ -222,6 +228,8 @@ struct BvhBuild {
     float4 *triV8;         // 3 * n, BVH8 leaf order
     int numNodes8;
     int levels8;
+    int levelOff8[258];    // first node of each BVH8 level; [levels8] = numNodes8
+    float *box8;           // refit: full-precision box (lo xyz, hi xyz) per BVH8 node (lazy)
 };
 // Collapses the BVH2 of `b` into b.nodes8 / b.triV8 (leaf sizes <= 4).
 int buildBvh8(BvhBuild &b, int numTris, cudaStream_t st);
@@ -230,3 +238,8 @@ int buildBvh8(BvhBuild &b, int numTris, cudaStream_t st);
 int buildBvh(const float *positions, const int *triIndices, const int *matIndices, const uint32_t *triFlags,
              int numTris, int leafSize, BvhBuild &out, cudaStream_t st);
 void freeBvh(BvhBuild &b);
+// Refits the BVH8 in place after the vertex positions changed: triangle
+// records regathered, then every level's quantised child boxes recomputed
+// from the deepest level up; topology, slots and leaf layout kept. Enqueued
+// on `st` without host synchronisation (capturable). 0 or a CUDA error.
+int refitBvh8(BvhBuild &b, const float *positions, const int *triIndices, int numTris, cudaStream_t st);

@@ -35,12 +35,14 @@
 // points and lines are skipped; .glb containers, data: URIs, unsigned byte
 // indices, normalised integer attributes and sparse accessors are read.
 // The file is compiled without floating-point contraction.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <new>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -430,7 +432,26 @@ struct Loader {
     int defaultMaterial = -1;
     bool camera = false;
     float camEye[3] = {0, 0, 0}, camTarget[3] = {0, 0, -1}, fovYDeg = 45.0f;
-    std::vector<Mat4> world;  // per glTF node
+    std::vector<Mat4> world;  // per glTF node, rest pose
+
+    // Deformation data: every emitted vertex in its shape's (mesh node's)
+    // space, the shape it belongs to and, for skinned shapes, four joint
+    // slots and weights. A shape's joint slots are its own (the joint
+    // matrices depend on the mesh node's world matrix).
+    std::vector<uint32_t> vShape;
+    std::vector<uint16_t> vJoints;
+    std::vector<float> vWeights;
+    bool anySkin = false;
+    struct Shape {
+        int node, skin, jointBase;
+    };
+    std::vector<Shape> shapes;
+    struct Skin {
+        std::vector<int> joints;
+        std::vector<Mat4> ibm;
+    };
+    std::map<int, Skin> skins;
+    int jointSlots = 0;
 
     Loader(Doc &doc, const float *upHint) : d(doc), up(upHint) {}
 
@@ -729,7 +750,7 @@ struct Loader {
         lights.push_back(L);
     }
 
-    bool primitive(const Json &pr, const Mat4 &w, const float nm[3][3], const std::vector<Mat4> *skin)
+    bool primitive(const Json &pr, uint32_t shape, bool skinned)
     {
         const int mode = inum(child(&pr, "mode"), 4);
         if (mode < 4)
@@ -749,13 +770,17 @@ struct Loader {
             return false;
         if ((na && nn != nv) || (ta && nt != nv))
             return d.err.set(OPTPT_ERR_PARSE, "primitive attributes of different lengths");
-        if (skin) {
+        if (skinned) {
             const Json *ja = child(at, "JOINTS_0"), *wa = child(at, "WEIGHTS_0");
             if (ja && wa) {
                 if (!d.readFloats(inum(ja, -1), 4, J, nj) || !d.readFloats(inum(wa, -1), 4, W, nw))
                     return false;
                 if (nj != nv || nw != nv)
                     return d.err.set(OPTPT_ERR_PARSE, "skin attributes of different lengths");
+                const size_t nJoints = skins[shapes[shape].skin].joints.size();
+                for (float j : J)
+                    if ((size_t)j >= nJoints)
+                        return d.err.set(OPTPT_ERR_PARSE, "joint index out of range");
             }
         }
         std::vector<uint32_t> ind;
@@ -787,76 +812,49 @@ struct Loader {
                 tri.push_back(ind[i]);
             }
         }
-        // World-space vertices.
-        std::vector<float> wp(nv * 3), wn(N.empty() ? 0 : nv * 3);
-        for (size_t v = 0; v < nv; ++v) {
-            const float p4[4] = {P[3 * v], P[3 * v + 1], P[3 * v + 2], 1.0f};
-            if (!J.empty()) {
-                Mat4 sm{};
-                for (int k = 0; k < 4; ++k) {
-                    const size_t j = (size_t)J[4 * v + k];
-                    const float wt = W[4 * v + k];
-                    if (wt == 0.0f)
-                        continue;
-                    if (j >= skin->size())
-                        return d.err.set(OPTPT_ERR_PARSE, "joint index out of range");
-                    for (int c = 0; c < 4; ++c)
-                        for (int r = 0; r < 4; ++r)
-                            sm.m[c][r] = sm.m[c][r] + wt * (*skin)[j].m[c][r];
-                }
-                float q[3];
-                xform(sm, p4, q);
-                const float q4[4] = {q[0], q[1], q[2], 1.0f};
-                xform(w, q4, &wp[3 * v]);
-            } else {
-                xform(w, p4, &wp[3 * v]);
-            }
-            if (!N.empty())
-                for (int r = 0; r < 3; ++r) {
-                    float s = nm[r][0] * N[3 * v];
-                    s = s + nm[r][1] * N[3 * v + 1];
-                    s = s + nm[r][2] * N[3 * v + 2];
-                    wn[3 * v + r] = s;
-                }
-        }
         const int m = materialOf(inum(child(&pr, "material"), -1));
-        const bool flat = anyNormals && N.empty();
-        if (flat) {
-            // Unindexed, each corner carrying the face normal.
+        const int jb = shapes[shape].jointBase;
+        auto vertex = [&](uint32_t vi, const float *normal) {
+            for (int q = 0; q < 3; ++q)
+                pos.push_back(P[3 * vi + q]);
+            if (anyNormals)
+                for (int q = 0; q < 3; ++q)
+                    nrm.push_back(normal ? normal[q] : N[3 * vi + q]);
+            if (anyTexCoords) {
+                tc.push_back(T.empty() ? 0.0f : T[2 * vi]);
+                tc.push_back(T.empty() ? 0.0f : T[2 * vi + 1]);
+            }
+            vShape.push_back(shape);
+            for (int k = 0; k < 4; ++k) {
+                vJoints.push_back(J.empty() ? (uint16_t)0 : (uint16_t)(jb + (int)J[4 * vi + k]));
+                vWeights.push_back(J.empty() ? 0.0f : W[4 * vi + k]);
+            }
+            anySkin |= !J.empty();
+        };
+        if (anyNormals && N.empty()) {
+            // Unindexed, each corner carrying the face normal (in the
+            // shape's space; it follows the shape's normal matrix).
             for (size_t t = 0; t + 2 < tri.size(); t += 3) {
-                const float *a = &wp[3 * tri[t]], *b = &wp[3 * tri[t + 1]], *c = &wp[3 * tri[t + 2]];
+                const float *a = &P[3 * tri[t]], *b = &P[3 * tri[t + 1]], *c = &P[3 * tri[t + 2]];
                 const double e1[3] = {(double)b[0] - a[0], (double)b[1] - a[1], (double)b[2] - a[2]};
                 const double e2[3] = {(double)c[0] - a[0], (double)c[1] - a[1], (double)c[2] - a[2]};
-                double fn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
-                                e1[0] * e2[1] - e1[1] * e2[0]};
+                const double fn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                      e1[0] * e2[1] - e1[1] * e2[0]};
                 const double l = std::sqrt(fn[0] * fn[0] + fn[1] * fn[1] + fn[2] * fn[2]);
-                const int32_t base = (int32_t)(pos.size() / 3);
+                const float f[3] = {l > 0 ? (float)(fn[0] / l) : 0.0f, l > 0 ? (float)(fn[1] / l) : 0.0f,
+                                    l > 0 ? (float)(fn[2] / l) : 0.0f};
+                const int32_t base = (int32_t)(vShape.size());
                 for (int k = 0; k < 3; ++k) {
-                    const uint32_t vi = tri[t + (size_t)k];
-                    for (int q = 0; q < 3; ++q) {
-                        pos.push_back(wp[3 * vi + q]);
-                        nrm.push_back(l > 0 ? (float)(fn[q] / l) : 0.0f);
-                    }
-                    if (anyTexCoords) {
-                        tc.push_back(T.empty() ? 0.0f : T[2 * vi]);
-                        tc.push_back(T.empty() ? 0.0f : T[2 * vi + 1]);
-                    }
+                    vertex(tri[t + (size_t)k], f);
                     idx.push_back(base + k);
                 }
                 mat.push_back(m);
             }
             return true;
         }
-        const int32_t base = (int32_t)(pos.size() / 3);
-        pos.insert(pos.end(), wp.begin(), wp.end());
-        if (anyNormals)
-            nrm.insert(nrm.end(), wn.begin(), wn.end());
-        if (anyTexCoords) {
-            if (T.empty())
-                tc.insert(tc.end(), nv * 2, 0.0f);
-            else
-                tc.insert(tc.end(), T.begin(), T.end());
-        }
+        const int32_t base = (int32_t)(vShape.size());
+        for (size_t v = 0; v < nv; ++v)
+            vertex((uint32_t)v, nullptr);
         for (size_t t = 0; t + 2 < tri.size(); t += 3) {
             for (int k = 0; k < 3; ++k)
                 idx.push_back(base + (int32_t)tri[t + (size_t)k]);
@@ -865,43 +863,35 @@ struct Loader {
         return true;
     }
 
-    bool skinMatrices(int skinIndex, const Mat4 &nodeWorld, std::vector<Mat4> &out)
+    bool loadSkin(int skinIndex)
     {
+        if (skins.count(skinIndex))
+            return true;
         const Json *sk = d.at("skins", skinIndex);
         const Json *joints = child(sk, "joints");
-        if (!sk || !joints)
+        if (!sk || !joints || !joints->isArr())
             return d.err.set(OPTPT_ERR_PARSE, "bad skin " + std::to_string(skinIndex));
-        const size_t nj = joints->arr.size();
-        std::vector<float> ibm;
-        size_t cnt = 0;
+        Skin S;
+        for (auto &j : joints->arr) {
+            const int jn = inum(&j, -1);
+            if (jn < 0 || (size_t)jn >= world.size())
+                return d.err.set(OPTPT_ERR_PARSE, "bad joint node");
+            S.joints.push_back(jn);
+        }
+        const size_t nj = S.joints.size();
+        S.ibm.assign(nj, Mat4::identity());
         if (const Json *ib = child(sk, "inverseBindMatrices")) {
+            std::vector<float> ibm;
+            size_t cnt = 0;
             if (!d.readFloats(inum(ib, -1), 16, ibm, cnt))
                 return false;
             if (cnt < nj)
                 return d.err.set(OPTPT_ERR_PARSE, "skin has fewer inverse bind matrices than joints");
-        }
-        // inverse(nodeWorld), in double.
-        double a[16], inv[16];
-        for (int c = 0; c < 4; ++c)
-            for (int r = 0; r < 4; ++r)
-                a[c * 4 + r] = nodeWorld.m[c][r];
-        if (!invert4(a, inv))
-            return d.err.set(OPTPT_ERR_PARSE, "singular node transform on a skinned mesh");
-        Mat4 iw;
-        for (int c = 0; c < 4; ++c)
-            for (int r = 0; r < 4; ++r)
-                iw.m[c][r] = (float)inv[c * 4 + r];
-        out.resize(nj);
-        for (size_t j = 0; j < nj; ++j) {
-            const int jn = inum(&joints->arr[j], -1);
-            if (jn < 0 || (size_t)jn >= world.size())
-                return d.err.set(OPTPT_ERR_PARSE, "bad joint node");
-            Mat4 b = Mat4::identity();
-            if (!ibm.empty())
+            for (size_t j = 0; j < nj; ++j)
                 for (int k = 0; k < 16; ++k)
-                    b.m[k / 4][k % 4] = ibm[j * 16 + (size_t)k];
-            out[j] = mul(mul(iw, world[(size_t)jn]), b);
+                    S.ibm[j].m[k / 4][k % 4] = ibm[j * 16 + (size_t)k];
         }
+        skins[skinIndex] = std::move(S);
         return true;
     }
 
@@ -966,15 +956,18 @@ struct Loader {
             const Json *mj = d.at("meshes", mesh);
             if (!mj)
                 return d.err.set(OPTPT_ERR_PARSE, "mesh " + std::to_string(mesh) + " missing");
-            float nm[3][3];
-            normalMatrix(w, nm);
-            std::vector<Mat4> skinM;
             const int skin = inum(child(node, "skin"), -1);
-            if (skin >= 0 && !skinMatrices(skin, w, skinM))
+            if (skin >= 0 && !loadSkin(skin))
                 return false;
+            shapes.push_back({n, skin, jointSlots});
+            if (skin >= 0)
+                jointSlots += (int)skins[skin].joints.size();
+            if (jointSlots > 65535)
+                return d.err.set(OPTPT_ERR_PARSE, "more than 65535 joint slots");
+            const uint32_t shape = (uint32_t)shapes.size() - 1;
             if (const Json *prims = child(mj, "primitives"))
                 for (auto &pr : prims->arr)
-                    if (!primitive(pr, w, nm, skin >= 0 ? &skinM : nullptr))
+                    if (!primitive(pr, shape, skin >= 0))
                         return false;
         }
         if (const Json *ch = child(node, "children"))
@@ -1004,6 +997,104 @@ struct Loader {
                 scan(inum(&c, -1), depth + 1);
     }
 };
+
+// ------------------------------------------------------------------ animation
+// Node transforms and one animation (the reference's loadAnimations,
+// src/gltf_loader.cpp:1390-1509: animation 2 when the file has three or
+// more, else animation 0), evaluated as Renderer::updateScene does
+// (src/renderer.cpp:1060-1182): channels set a node's translation, rotation
+// or scale (STEP holds the previous key, LINEAR mixes, rotations slerp);
+// time wraps modulo each channel's last key time; world matrices are
+// recomputed down the tree (nodes with a "matrix" keep it); a shape's
+// vertices go through world * skin, with skin = sum of weight * joint matrix
+// and joint matrix = inverse(world(mesh node)) * world(joint) *
+// inverseBind; normals go through the inverse transpose of the mesh node's
+// world matrix only. Differences: CUBICSPLINE channels use the glTF cubic
+// Hermite spline (the reference's string test never matches them and reads
+// tangents as values); before the first key and at the last key the first
+// / last value is held (the reference divides by zero before the first key
+// and jumps to the first value at the last).
+struct Channel {
+    int node = -1, path = 0, interp = 1;  // path 0 T, 1 R, 2 S; interp 0 STEP, 1 LINEAR, 2 CUBICSPLINE
+    std::vector<float> t, v;              // v: comps per key (x3 for CUBICSPLINE: in-tangent, value, out-tangent)
+};
+
+struct NodeTRS {
+    bool hasMatrix = false;
+    Mat4 matrix = Mat4::identity();
+    float t[3] = {0, 0, 0}, r[4] = {0, 0, 0, 1}, s[3] = {1, 1, 1};
+    std::vector<int> children;
+};
+
+float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+
+void slerp(const float *x, const float *y, float a, float *out)
+{
+    float z[4] = {y[0], y[1], y[2], y[3]};
+    float c = x[0] * y[0] + x[1] * y[1] + x[2] * y[2] + x[3] * y[3];
+    if (c < 0.0f) {
+        for (int k = 0; k < 4; ++k)
+            z[k] = -z[k];
+        c = -c;
+    }
+    if (c > 1.0f - 1.1920929e-07f) {  // nearly parallel: linear
+        for (int k = 0; k < 4; ++k)
+            out[k] = mixf(x[k], z[k], a);
+        return;
+    }
+    const float angle = std::acos(c), sa = std::sin(angle);
+    const float wa = std::sin((1.0f - a) * angle), wb = std::sin(a * angle);
+    for (int k = 0; k < 4; ++k)
+        out[k] = (wa * x[k] + wb * z[k]) / sa;
+}
+
+void sampleChannel(const Channel &ch, float time, float *out)
+{
+    const int comps = ch.path == 1 ? 4 : 3;
+    const size_t n = ch.t.size();
+    const int stride = ch.interp == 2 ? 3 * comps : comps, off = ch.interp == 2 ? comps : 0;
+    auto key = [&](size_t i) { return &ch.v[i * (size_t)stride + (size_t)off]; };
+    float t = time;
+    const float tmax = ch.t[n - 1];
+    if (tmax > 0.0f && t > tmax) {
+        float ip;
+        t = std::modf(t / tmax, &ip) * tmax;
+    }
+    size_t next = n;
+    for (size_t i = 0; i < n; ++i)
+        if (ch.t[i] > t) {
+            next = i;
+            break;
+        }
+    if (next == 0 || next == n || ch.interp == 0) {
+        const size_t i = next == 0 ? 0 : next == n ? n - 1 : next - 1;
+        memcpy(out, key(i), sizeof(float) * (size_t)comps);
+        return;
+    }
+    const size_t prev = next - 1;
+    const float td = ch.t[next] - ch.t[prev];
+    const float a = (t - ch.t[prev]) / td;
+    if (ch.interp == 2) {
+        const float a2 = a * a, a3 = a2 * a;
+        const float h00 = 2 * a3 - 3 * a2 + 1, h10 = a3 - 2 * a2 + a, h01 = -2 * a3 + 3 * a2, h11 = a3 - a2;
+        const float *v0 = key(prev), *v1 = key(next);
+        const float *b0 = v0 + comps, *a1 = v1 - comps;  // out-tangent of prev, in-tangent of next
+        for (int k = 0; k < comps; ++k)
+            out[k] = h00 * v0[k] + h10 * td * b0[k] + h01 * v1[k] + h11 * td * a1[k];
+        if (comps == 4) {
+            const float l = std::sqrt(out[0] * out[0] + out[1] * out[1] + out[2] * out[2] + out[3] * out[3]);
+            for (int k = 0; k < 4 && l > 0; ++k)
+                out[k] /= l;
+        }
+        return;
+    }
+    if (comps == 4) {
+        slerp(key(prev), key(next), a, out);
+        return;
+    }
+    for (int k = 0; k < 3; ++k)
+        out[k] = mixf(key(prev)[k], key(next)[k], a);
+}
 
 template <class T> T *dupv(const std::vector<T> &v)
 {
@@ -1065,13 +1156,157 @@ int parseDocument(const std::string &path, Doc &d)
 
 }  // namespace
 
-extern "C" {
+// A loaded glTF scene: the flattened static data plus what is needed to pose
+// it at any time (node tree, skins, one animation, per-vertex bindings).
+struct optpt_gltf {
+    std::vector<float> restPos, restNrm, tc;
+    std::vector<int32_t> idx, mat;
+    std::vector<MaterialData> materials;
+    std::vector<Light> lights;
+    std::vector<optpt_texture> textures;  // pixels owned here until handed to a scene
+    float camEye[3], camTarget[3], camUp[3], fovYDeg;
+    bool anyNormals = false, anyTexCoords = false, anySkin = false;
+    std::vector<uint32_t> vShape;
+    std::vector<uint16_t> vJoints;
+    std::vector<float> vWeights;
+    struct Shape {
+        int node, skin, jointBase;
+    };
+    std::vector<Shape> shapes;
+    std::map<int, std::pair<std::vector<int>, std::vector<Mat4>>> skins;  // joints, inverse binds
+    int jointSlots = 0;
+    std::vector<NodeTRS> nodes;
+    std::vector<int> roots;
+    std::vector<Channel> channels;
+    float duration = 0.0f;
 
-int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *out)
+    ~optpt_gltf()
+    {
+        for (auto &t : textures)
+            free((void *)t.rgba);
+    }
+
+    void worlds(int n, const Mat4 &parent, const std::vector<NodeTRS> &cur, std::vector<Mat4> &w, int depth) const
+    {
+        if (n < 0 || (size_t)n >= cur.size() || depth > 256)
+            return;
+        const NodeTRS &N = cur[(size_t)n];
+        Mat4 local = N.matrix;
+        if (!N.hasMatrix) {
+            Mat4 t = Mat4::identity(), s = Mat4::identity();
+            for (int k = 0; k < 3; ++k) {
+                t.m[3][k] = N.t[k];
+                s.m[k][k] = N.s[k];
+            }
+            local = mul(mul(t, fromQuat(N.r[0], N.r[1], N.r[2], N.r[3])), s);
+        }
+        w[(size_t)n] = mul(parent, local);
+        for (int c : N.children)
+            worlds(c, w[(size_t)n], cur, w, depth + 1);
+    }
+
+    // Shape matrices (16 per shape), shape normal matrices (9 per shape, row
+    // r multiplies the normal), joint matrices (16 per slot), at `time`
+    // (animation applied when animate).
+    bool pose(float time, bool animate, float *shapeM, float *shapeN, float *jointM) const
+    {
+        std::vector<NodeTRS> cur = nodes;
+        if (animate)
+            for (const Channel &ch : channels) {
+                float v[4];
+                sampleChannel(ch, time, v);
+                NodeTRS &N = cur[(size_t)ch.node];
+                if (ch.path == 0)
+                    memcpy(N.t, v, 12);
+                else if (ch.path == 1)
+                    memcpy(N.r, v, 16);
+                else
+                    memcpy(N.s, v, 12);
+            }
+        std::vector<Mat4> w(cur.size(), Mat4::identity());
+        for (int r : roots)
+            worlds(r, Mat4::identity(), cur, w, 0);
+        for (size_t s = 0; s < shapes.size(); ++s) {
+            const Mat4 &G = w[(size_t)shapes[s].node];
+            if (shapeM)
+                memcpy(shapeM + 16 * s, G.m, 64);
+            if (shapeN) {
+                float nm[3][3];
+                normalMatrix(G, nm);
+                memcpy(shapeN + 9 * s, nm, 36);
+            }
+            if (jointM && shapes[s].skin >= 0) {
+                const auto &sk = skins.at(shapes[s].skin);
+                double a[16], inv[16];
+                for (int c = 0; c < 4; ++c)
+                    for (int r = 0; r < 4; ++r)
+                        a[c * 4 + r] = G.m[c][r];
+                if (!Loader::invert4(a, inv))
+                    return false;
+                Mat4 iw;
+                for (int c = 0; c < 4; ++c)
+                    for (int r = 0; r < 4; ++r)
+                        iw.m[c][r] = (float)inv[c * 4 + r];
+                for (size_t j = 0; j < sk.first.size(); ++j) {
+                    const Mat4 J = mul(mul(iw, w[(size_t)sk.first[j]]), sk.second[j]);
+                    memcpy(jointM + 16 * ((size_t)shapes[s].jointBase + j), J.m, 64);
+                }
+            }
+        }
+        return true;
+    }
+};
+
+// The vertex transform the GPU deformation kernel applies, in the same
+// float operations (this file is compiled without contraction).
+static void deformVertex(const float *p, const float *n, uint32_t shape, const uint16_t *joints, const float *weights,
+                  const float *shapeM, const float *shapeN, const float *jointM, float *outP, float *outN)
 {
-    if (!path || !out)
-        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
-    memset(out, 0, sizeof(*out));
+    const float *G = shapeM + 16 * (size_t)shape;
+    float P[16];
+    if (joints) {
+        float S[16];
+        for (int e = 0; e < 16; ++e) {
+            float acc = weights[0] * jointM[16 * (size_t)joints[0] + e];
+            acc = acc + weights[1] * jointM[16 * (size_t)joints[1] + e];
+            acc = acc + weights[2] * jointM[16 * (size_t)joints[2] + e];
+            acc = acc + weights[3] * jointM[16 * (size_t)joints[3] + e];
+            S[e] = acc;
+        }
+        for (int c = 0; c < 4; ++c)
+            for (int r = 0; r < 4; ++r) {
+                float acc = G[0 * 4 + r] * S[c * 4 + 0];
+                acc = acc + G[1 * 4 + r] * S[c * 4 + 1];
+                acc = acc + G[2 * 4 + r] * S[c * 4 + 2];
+                acc = acc + G[3 * 4 + r] * S[c * 4 + 3];
+                P[c * 4 + r] = acc;
+            }
+    } else {
+        memcpy(P, G, 64);
+    }
+    for (int r = 0; r < 3; ++r) {
+        float acc = P[0 * 4 + r] * p[0];
+        acc = acc + P[1 * 4 + r] * p[1];
+        acc = acc + P[2 * 4 + r] * p[2];
+        acc = acc + P[3 * 4 + r];
+        outP[r] = acc;
+    }
+    if (n && outN) {
+        const float *N = shapeN + 9 * (size_t)shape;
+        for (int r = 0; r < 3; ++r) {
+            float acc = N[3 * r] * n[0];
+            acc = acc + N[3 * r + 1] * n[1];
+            acc = acc + N[3 * r + 2] * n[2];
+            outN[r] = acc;
+        }
+    }
+}
+
+namespace {
+
+int loadModel(const char *path, const float upHint[3], optpt_gltf *&out)
+{
+    out = nullptr;
     Doc d;
     int rc = parseDocument(path, d);
     if (rc)
@@ -1085,12 +1320,11 @@ int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *
     const float defaultUp[3] = {0, 1, 0};
     Loader L(d, upHint ? upHint : defaultUp);
     const Json *nodes = d.j.get("nodes");
-    L.world.assign(nodes && nodes->isArr() ? nodes->arr.size() : 0, Mat4::identity());
+    const size_t numNodes = nodes && nodes->isArr() ? nodes->arr.size() : 0;
+    L.world.assign(numNodes, Mat4::identity());
     bool ok = L.loadMaterials();
     const Json *roots = child(scene, "nodes");
     if (ok && roots) {
-        // World matrices of every root tree of the document (joints may sit
-        // outside the default scene's own trees).
         for (auto &r : roots->arr)
             if (!(ok = L.worlds(inum(&r, -1), Mat4::identity(), 0)))
                 break;
@@ -1102,30 +1336,184 @@ int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *
                 if (!(ok = L.visit(inum(&r, -1), 0)))
                     break;
     }
-    if (!ok) {
+    optpt_gltf *g = new (std::nothrow) optpt_gltf();
+    if (!g) {
         for (auto &t : L.textures)
             free((void *)t.rgba);
+        return optpt_internal_set_error(OPTPT_ERR_NOMEM, "glTF model allocation failed");
+    }
+    g->textures.swap(L.textures);  // owned (and freed) by g from here on
+    // Node tree with rest transforms, and the animation's channels.
+    g->nodes.resize(numNodes);
+    for (size_t n = 0; ok && n < numNodes; ++n) {
+        const Json &nj = nodes->arr[n];
+        NodeTRS &N = g->nodes[n];
+        const Json *m = child(&nj, "matrix");
+        if (m && m->isArr() && m->arr.size() == 16) {
+            N.hasMatrix = true;
+            for (int i = 0; i < 16; ++i)
+                N.matrix.m[i / 4][i % 4] = (float)num(&m->arr[(size_t)i], 0);
+        }
+        auto vec = [&](const char *k, float *dst, size_t len, float dflt) {
+            const Json *v = child(&nj, k);
+            if (v && v->isArr() && v->arr.size() == len)
+                for (size_t i = 0; i < len; ++i)
+                    dst[i] = (float)num(&v->arr[i], dflt);
+        };
+        vec("translation", N.t, 3, 0.0f);
+        vec("rotation", N.r, 4, 0.0f);
+        vec("scale", N.s, 3, 1.0f);
+        if (const Json *ch = child(&nj, "children"))
+            for (auto &c : ch->arr) {
+                const int ci = inum(&c, -1);
+                if (ci < 0 || (size_t)ci >= numNodes) {
+                    ok = d.err.set(OPTPT_ERR_PARSE, "bad child node");
+                    break;
+                }
+                N.children.push_back(ci);
+            }
+    }
+    if (ok && roots)
+        for (auto &r : roots->arr)
+            g->roots.push_back(inum(&r, -1));
+    const Json *anims = d.j.get("animations");
+    if (ok && anims && anims->isArr() && !anims->arr.empty()) {
+        const Json &an = anims->arr[anims->arr.size() >= 3 ? 2 : 0];
+        const Json *samplers = child(&an, "samplers"), *chans = child(&an, "channels");
+        if (chans && chans->isArr())
+            for (auto &cj : chans->arr) {
+                const Json *tgt = child(&cj, "target");
+                const Json *pathJ = child(tgt, "path");
+                const int node = inum(child(tgt, "node"), -1);
+                const std::string path = pathJ && pathJ->isStr() ? pathJ->str : "";
+                const int p = path == "translation" ? 0 : path == "rotation" ? 1 : path == "scale" ? 2 : -1;
+                if (p < 0 || node < 0 || (size_t)node >= numNodes)
+                    continue;  // morph-target weights and the like are not animated
+                const Json *sj = elem(samplers, inum(child(&cj, "sampler"), -1));
+                if (!sj) {
+                    ok = d.err.set(OPTPT_ERR_PARSE, "animation channel without sampler");
+                    break;
+                }
+                Channel ch;
+                ch.node = node;
+                ch.path = p;
+                const Json *ij = child(sj, "interpolation");
+                const std::string interp = ij && ij->isStr() ? ij->str : "LINEAR";
+                ch.interp = interp == "STEP" ? 0 : interp == "CUBICSPLINE" ? 2 : 1;
+                size_t nt = 0, nv = 0;
+                if (!d.readFloats(inum(child(sj, "input"), -1), 1, ch.t, nt) ||
+                    !d.readFloats(inum(child(sj, "output"), -1), p == 1 ? 4 : 3, ch.v, nv)) {
+                    ok = false;
+                    break;
+                }
+                if (nt == 0 || nv != nt * (ch.interp == 2 ? 3u : 1u)) {
+                    ok = d.err.set(OPTPT_ERR_PARSE, "animation sampler input/output counts differ");
+                    break;
+                }
+                for (size_t i = 1; i < nt; ++i)
+                    if (!(ch.t[i] > ch.t[i - 1])) {
+                        ok = d.err.set(OPTPT_ERR_PARSE, "animation key times must increase");
+                        break;
+                    }
+                if (!ok)
+                    break;
+                g->duration = std::max(g->duration, ch.t.back());
+                g->channels.push_back(std::move(ch));
+            }
+    }
+    if (!ok) {
+        delete g;
         return optpt_internal_set_error(d.err.code ? d.err.code : OPTPT_ERR_PARSE, d.err.msg.c_str());
     }
-    out->positions = dupv(L.pos);
-    out->numVertices = (uint32_t)(L.pos.size() / 3);
-    out->normals = L.anyNormals ? dupv(L.nrm) : nullptr;
-    out->texCoords = L.anyTexCoords ? dupv(L.tc) : nullptr;
-    out->triIndices = dupv(L.idx);
-    out->numTriangles = (uint32_t)L.mat.size();
-    out->matIndices = dupv(L.mat);
-    out->materials = dupv(L.materials);
-    out->numMaterials = (uint32_t)L.materials.size();
-    out->lights = dupv(L.lights);
-    out->numLights = (uint32_t)L.lights.size();
-    out->textures = dupv(L.textures);
-    out->numTextures = (uint32_t)L.textures.size();
+    g->restPos.swap(L.pos);
+    g->restNrm.swap(L.nrm);
+    g->tc.swap(L.tc);
+    g->idx.swap(L.idx);
+    g->mat.swap(L.mat);
+    g->materials.swap(L.materials);
+    g->lights.swap(L.lights);
     for (int k = 0; k < 3; ++k) {
-        out->camEye[k] = L.camEye[k];
-        out->camTarget[k] = L.camTarget[k];
-        out->camUp[k] = L.up[k];
+        g->camEye[k] = L.camEye[k];
+        g->camTarget[k] = L.camTarget[k];
+        g->camUp[k] = L.up[k];
     }
-    out->camFovYDeg = L.fovYDeg;
+    g->fovYDeg = L.fovYDeg;
+    g->anyNormals = L.anyNormals;
+    g->anyTexCoords = L.anyTexCoords;
+    g->anySkin = L.anySkin;
+    g->vShape.swap(L.vShape);
+    g->vJoints.swap(L.vJoints);
+    g->vWeights.swap(L.vWeights);
+    for (auto &s : L.shapes)
+        g->shapes.push_back({s.node, s.skin, s.jointBase});
+    for (auto &kv : L.skins)
+        g->skins[kv.first] = {kv.second.joints, kv.second.ibm};
+    g->jointSlots = L.jointSlots;
+    out = g;
+    return OPTPT_OK;
+}
+
+// Positions and normals of every vertex at `time` on the host.
+int applyPose(const optpt_gltf *g, float time, bool animate, float *positions, float *normals)
+{
+    std::vector<float> M(16 * g->shapes.size()), N(9 * g->shapes.size()), J(16 * (size_t)g->jointSlots);
+    if (!g->pose(time, animate, M.data(), N.data(), J.data()))
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "singular node transform on a skinned mesh");
+    const size_t nv = g->vShape.size();
+    for (size_t v = 0; v < nv; ++v) {
+        // A vertex follows its skin when it has a non-zero weight (a skinned
+        // primitive without JOINTS_0 / WEIGHTS_0 stays rigid with its node).
+        const float *w = &g->vWeights[4 * v];
+        const bool skinned = g->anySkin && g->shapes[g->vShape[v]].skin >= 0 &&
+                             (w[0] != 0.0f || w[1] != 0.0f || w[2] != 0.0f || w[3] != 0.0f);
+        deformVertex(&g->restPos[3 * v], g->anyNormals ? &g->restNrm[3 * v] : nullptr, g->vShape[v],
+                     skinned ? &g->vJoints[4 * v] : nullptr, skinned ? &g->vWeights[4 * v] : nullptr, M.data(),
+                     N.data(), J.data(), positions + 3 * v, normals ? normals + 3 * v : nullptr);
+    }
+    return OPTPT_OK;
+}
+
+// The model's scene at `time`; textures are copied (the model keeps its own).
+int sceneOf(const optpt_gltf *g, float time, bool animate, optpt_scene *out)
+{
+    memset(out, 0, sizeof(*out));
+    const size_t nv = g->vShape.size();
+    std::vector<float> P(3 * nv), Nn(g->anyNormals ? 3 * nv : 0);
+    int rc = applyPose(g, time, animate, P.data(), g->anyNormals ? Nn.data() : nullptr);
+    if (rc)
+        return rc;
+    std::vector<optpt_texture> tex = g->textures;
+    for (auto &t : tex) {
+        const size_t bytes = (size_t)t.width * t.height * 4;
+        uint8_t *px = (uint8_t *)malloc(bytes ? bytes : 1);
+        if (!px) {
+            for (auto &u : tex)
+                if (&u != &t && u.rgba != nullptr && (&u < &t))
+                    free((void *)u.rgba);
+            return optpt_internal_set_error(OPTPT_ERR_NOMEM, "texture allocation failed");
+        }
+        memcpy(px, t.rgba, bytes);
+        t.rgba = px;
+    }
+    out->positions = dupv(P);
+    out->numVertices = (uint32_t)nv;
+    out->normals = g->anyNormals ? dupv(Nn) : nullptr;
+    out->texCoords = g->anyTexCoords ? dupv(g->tc) : nullptr;
+    out->triIndices = dupv(g->idx);
+    out->numTriangles = (uint32_t)g->mat.size();
+    out->matIndices = dupv(g->mat);
+    out->materials = dupv(g->materials);
+    out->numMaterials = (uint32_t)g->materials.size();
+    out->lights = dupv(g->lights);
+    out->numLights = (uint32_t)g->lights.size();
+    out->textures = dupv(tex);
+    out->numTextures = (uint32_t)tex.size();
+    for (int k = 0; k < 3; ++k) {
+        out->camEye[k] = g->camEye[k];
+        out->camTarget[k] = g->camTarget[k];
+        out->camUp[k] = g->camUp[k];
+    }
+    out->camFovYDeg = g->fovYDeg;
     out->resX = 1280;
     out->resY = 720;
     out->spp = 64;
@@ -1133,7 +1521,89 @@ int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *
     return OPTPT_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *out)
+{
+    if (!path || !out)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    memset(out, 0, sizeof(*out));
+    optpt_gltf *g = nullptr;
+    int rc = loadModel(path, upHint, g);
+    if (rc)
+        return rc;
+    rc = sceneOf(g, 0.0f, false, out);
+    delete g;
+    return rc;
+}
+
+int optpt_gltf_open(const char *path, const float upHint[3], optpt_gltf **out)
+{
+    if (!path || !out)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    return loadModel(path, upHint, *out);
+}
+
+void optpt_gltf_close(optpt_gltf *g) { delete g; }
+
+int optpt_gltf_scene(const optpt_gltf *g, float time, int animate, optpt_scene *out)
+{
+    if (!g || !out)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    return sceneOf(g, time, animate != 0, out);
+}
+
+int optpt_gltf_info(const optpt_gltf *g, optpt_gltf_info_t *info)
+{
+    if (!g || !info)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    info->numVertices = (uint32_t)g->vShape.size();
+    info->numShapes = (uint32_t)g->shapes.size();
+    info->numJointSlots = (uint32_t)g->jointSlots;
+    info->numChannels = (uint32_t)g->channels.size();
+    info->duration = g->duration;
+    info->skinned = g->anySkin ? 1 : 0;
+    return OPTPT_OK;
+}
+
+int optpt_gltf_deformation(const optpt_gltf *g, optpt_deformation *out)
+{
+    if (!g || !out)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    memset(out, 0, sizeof(*out));
+    out->restPositions = g->restPos.data();
+    out->restNormals = g->anyNormals ? g->restNrm.data() : nullptr;
+    out->vertexShape = g->vShape.data();
+    out->joints = g->anySkin ? g->vJoints.data() : nullptr;
+    out->weights = g->anySkin ? g->vWeights.data() : nullptr;
+    out->numVertices = (uint32_t)g->vShape.size();
+    out->numShapes = (uint32_t)g->shapes.size();
+    out->numJoints = (uint32_t)g->jointSlots;
+    return OPTPT_OK;
+}
+
+int optpt_gltf_pose(const optpt_gltf *g, float time, float *shapeMatrices, float *shapeNormalMatrices,
+                    float *jointMatrices)
+{
+    if (!g)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    if (!g->pose(time, true, shapeMatrices, shapeNormalMatrices, jointMatrices))
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "singular node transform on a skinned mesh");
+    return OPTPT_OK;
+}
+
+int optpt_gltf_apply(const optpt_gltf *g, float time, float *positions, float *normals)
+{
+    if (!g || !positions)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    return applyPose(g, time, true, positions, normals);
+}
+
 int optpt_image_decode_png(const void *data, size_t size, optpt_image *out)
+
 {
     if (!data || !out)
         return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");

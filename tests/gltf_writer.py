@@ -327,3 +327,102 @@ def from_scene(scene):
             start = k
     g.node(mesh=g.mesh(prims))
     return g
+
+
+def _box(c, h):
+    """12-triangle box (24 vertices with face normals) centred at c, half size h."""
+    c, h = np.asarray(c, np.float32), np.asarray(h, np.float32)
+    P, N, I = [], [], []
+    for ax in range(3):
+        for sgn in (-1.0, 1.0):
+            n = np.zeros(3, np.float32)
+            n[ax] = sgn
+            u = np.zeros(3, np.float32)
+            u[(ax + 1) % 3] = 1
+            v = np.cross(n, u)
+            base = len(P)
+            for a, b in ((-1, -1), (1, -1), (1, 1), (-1, 1)):
+                P.append(c + h * (n + a * u + b * v))
+                N.append(n)
+            I += [base, base + 1, base + 2, base, base + 2, base + 3]
+    return np.array(P, np.float32), np.array(N, np.float32), np.array(I, np.uint32)
+
+
+def animated_scene(num_animations=3):
+    """A small animated document: a rotating arm carrying a box that steps
+    along (node translation STEP), a skinned strip bent by two animated
+    joints (rotation LINEAR, scale CUBICSPLINE), a static ground and an
+    emissive panel on the arm. The animation that moves things is the one
+    the reference selects (index 2 when there are three or more, else 0);
+    the others move the ground, which must therefore stay still."""
+    g = Gltf()
+    grey = g.material(pbrMetallicRoughness={"baseColorFactor": [0.7, 0.7, 0.7, 1], "metallicFactor": 0.0},
+                      extensions={"KHR_materials_specular": {"specularFactor": 0.0}})
+    red = g.material(pbrMetallicRoughness={"baseColorFactor": [0.8, 0.2, 0.1, 1], "metallicFactor": 0.0,
+                                           "roughnessFactor": 0.5})
+    lamp = g.material(emissiveFactor=[1.0, 1.0, 0.9], extensions={"KHR_materials_emissive_strength":
+                                                                  {"emissiveStrength": 8.0}})
+    bp, bn, bi = _box([0, 0, 0], [0.3, 0.3, 0.3])
+    box = g.mesh([g.primitive(bp, bi, bn, material=red)])
+    panel = g.mesh([g.primitive(np.array([[-0.3, 0, -0.3], [0.3, 0, -0.3], [0.3, 0, 0.3], [-0.3, 0, 0.3]],
+                                         np.float32), np.array([0, 2, 1, 0, 3, 2], np.uint32),
+                                np.tile(np.array([[0, -1, 0]], np.float32), (4, 1)), material=lamp)])
+    # skinned strip along x in [-1, 1], 9 columns x 2 rows
+    xs = np.linspace(-1, 1, 9, dtype=np.float32)
+    sp = np.array([[x, 0.0, z] for x in xs for z in (-0.2, 0.2)], np.float32)
+    sn = np.tile(np.array([[0, 1, 0]], np.float32), (len(sp), 1))
+    si = []
+    for k in range(8):
+        a, b, c, d = 2 * k, 2 * k + 1, 2 * k + 2, 2 * k + 3
+        si += [a, b, d, a, d, c]
+    w1 = np.clip((sp[:, 0] + 1) / 2, 0, 1)
+    joints = np.tile(np.array([[0, 1, 0, 0]], np.uint16), (len(sp), 1))
+    weights = np.stack([1 - w1, w1, np.zeros_like(w1), np.zeros_like(w1)], 1).astype(np.float32)
+    strip = g.primitive(sp, np.array(si, np.uint32), sn, material=grey)
+    strip["attributes"]["JOINTS_0"] = g.accessor(joints, 5123)
+    strip["attributes"]["WEIGHTS_0"] = g.accessor(weights)
+    strip_mesh = g.mesh([strip])
+    gp = np.array([[-3, 0, -3], [3, 0, -3], [3, 0, 3], [-3, 0, 3]], np.float32)
+    ground = g.mesh([g.primitive(gp, np.array([0, 2, 1, 0, 3, 2], np.uint32),
+                                 np.tile(np.array([[0, 1, 0]], np.float32), (4, 1)), material=grey)])
+    box_node = g.node(root=False, mesh=box, translation=[1.0, 0.5, 0.0])
+    panel_node = g.node(root=False, mesh=panel, translation=[0.0, 2.0, 0.0])
+    arm = g.node(children=[box_node, panel_node], translation=[0.0, 0.2, 0.0])
+    bone0 = g.node(root=False, translation=[-1.0, 0.0, 0.0])
+    bone1 = g.node(root=False, translation=[2.0, 0.0, 0.0])
+    g.doc["nodes"][bone0]["children"] = [bone1]
+    ibm = np.stack([np.eye(4), np.eye(4)]).astype(np.float32)
+    ibm[0][3, :3] = [1.0, 0, 0]   # column-major: translations in the last column
+    ibm[1][3, :3] = [-1.0, 0, 0]
+    g.doc["skins"] = [{"joints": [bone0, bone1], "inverseBindMatrices": g.accessor(ibm.reshape(2, 16), typ="MAT4")}]
+    strip_node = g.node(mesh=strip_mesh, skin=0, translation=[0.0, 1.0, -1.0])
+    rig = g.node(children=[bone0], translation=[0.0, 1.0, -1.0])
+    ground_node = g.node(mesh=ground)
+
+    def sampler(times, values, interp):
+        t = g.accessor(np.asarray(times, np.float32).reshape(-1))
+        v = g.accessor(np.asarray(values, np.float32))
+        return {"input": t, "output": v, "interpolation": interp}
+
+    s2, c2 = 0.7071067811865476, 0.7071067811865476
+    moving = {"samplers": [
+        sampler([0.0, 1.0, 2.0], [[0, 0, 0, 1], [0, s2, 0, c2], [0, 1, 0, 0]], "LINEAR"),            # arm yaw
+        sampler([0.5, 1.5], [[1.0, 0.5, 0.0], [1.5, 0.8, 0.3]], "STEP"),                              # box steps
+        sampler([0.0, 1.0, 2.0], [[0, 0, 0, 1], [0, 0, 0.3826834, 0.9238795], [0, 0, 0, 1]], "LINEAR"),  # bone0 bend
+        sampler([0.0, 1.0, 2.0],                                                                        # bone1 scale
+                [[0, 0, 0], [1, 1, 1], [0.5, 0, 0], [-0.5, 0, 0], [1.5, 1, 1], [0, 0, 0],
+                 [0, 0, 0], [1, 1, 1], [0, 0, 0]], "CUBICSPLINE")],
+        "channels": [{"sampler": 0, "target": {"node": arm, "path": "rotation"}},
+                     {"sampler": 1, "target": {"node": box_node, "path": "translation"}},
+                     {"sampler": 2, "target": {"node": bone0, "path": "rotation"}},
+                     {"sampler": 3, "target": {"node": bone1, "path": "scale"}}]}
+    decoy = {"samplers": [sampler([0.0, 1.0], [[0, 0, 0], [0, 5, 0]], "LINEAR")],
+             "channels": [{"sampler": 0, "target": {"node": ground_node, "path": "translation"}}]}
+    anims = [decoy] * num_animations
+    anims[2 if num_animations >= 3 else 0] = moving
+    g.doc["animations"] = anims
+    cam = g.camera(0.8)
+    g.node(translation=[0.0, 2.0, 5.0], rotation=[-0.1305262, 0, 0, 0.9914449], camera=cam)
+    g.light(type="point", intensity=3000.0)
+    g.node(translation=[2.0, 3.0, 2.0], extensions={"KHR_lights_punctual": {"light": 0}})
+    return g
