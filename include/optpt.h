@@ -528,7 +528,7 @@ int optpt_set_guiding(optpt_renderer *r, int mode);
  * trainStride  one path in trainStride records training samples (1)
  * maxDepth     vertices up to this depth are guided (all)
  * alphaMin     floor (0) and
- * alphaMax     cap (0.9) on the probability of sampling the network's
+ * alphaMax     cap (0.6) on the probability of sampling the network's
  *              mixture instead of the BSDF; between them that probability is
  *              the network's own (a learned output), phased in linearly ...
  * alphaRamp    ... over this many training steps (64)
@@ -536,7 +536,18 @@ int optpt_set_guiding(optpt_renderer *r, int mode);
  * lobeLoss     1: the lobes learn the part of the target the BSDF leaves
  *              (the loss of the whole proposal); 2: the whole target (2);
  *              the selection probability always learns from the loss of the
- *              whole proposal */
+ *              whole proposal
+ * trainSpp     in mode 1, online training stops (the network freezes) once
+ *              this many samples per pixel have been rendered with it,
+ *              counted from when this value is set or the network created
+ *              (0xFFFFFFFF: never stops, the default)
+ * primaryShare 1: the first hits of one pixel in a pass share one network
+ *              query, its first sample's (the proposal stays exact for every
+ *              sample: sampling and density use the same mixture; a quarter
+ *              of the inference time on the interior at 320 x 180, but
+ *              samples whose first hit lands on another surface than the
+ *              first sample's get a worse proposal); -1: one query per
+ *              sample, the default. */
 typedef struct optpt_guiding_options {
     uint32_t trainSteps;
     uint32_t trainStride;
@@ -546,6 +557,8 @@ typedef struct optpt_guiding_options {
     float alphaRamp;
     float learningRate;
     int32_t lobeLoss;
+    uint32_t trainSpp;
+    int32_t primaryShare;
 } optpt_guiding_options;
 int optpt_set_guiding_options(optpt_renderer *r, const optpt_guiding_options *o);
 int optpt_get_guiding_options(const optpt_renderer *r, optpt_guiding_options *o);

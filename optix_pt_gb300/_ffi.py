@@ -129,7 +129,8 @@ class KernelTimes(ctypes.Structure):
 class GuidingOptions(ctypes.Structure):
     _fields_ = [("trainSteps", ctypes.c_uint32), ("trainStride", ctypes.c_uint32), ("maxDepth", ctypes.c_uint32),
                 ("alphaMin", ctypes.c_float), ("alphaMax", ctypes.c_float), ("alphaRamp", ctypes.c_float),
-                ("learningRate", ctypes.c_float), ("lobeLoss", ctypes.c_int32)]
+                ("learningRate", ctypes.c_float), ("lobeLoss", ctypes.c_int32), ("trainSpp", ctypes.c_uint32),
+                ("primaryShare", ctypes.c_int32)]
 
 
 class AutotuneRequest(ctypes.Structure):

@@ -107,7 +107,12 @@ struct optpt_renderer {
     uint32_t *gBatchCount = nullptr;
     size_t gMixPaths = 0, gRecSlots = 0;
     uint32_t gTrainStride = 1, gBatchCap = 1u << 18, gTrainSteps = 4, gMaxDepth = 0xFFFFFFFFu;
-    float gAlphaMin = 0.0f, gAlphaMax = 0.9f, gAlphaRamp = 64.0f, gLr = 1e-2f;
+    uint32_t gTrainSpp = 0xFFFFFFFFu;  // online training stops after this many samples per pixel
+    bool gSharePrimary = false;        // a pixel's primary hits share one mixture per pass
+    uint64_t gTrainedSpp = 0;          // samples per pixel rendered with training so far
+    bool graphTrain = false;           // training state the captured pass was recorded with
+    bool trainingOpen() const { return guideMode == 1 && gTrainedSpp < gTrainSpp; }
+    float gAlphaMin = 0.0f, gAlphaMax = 0.6f, gAlphaRamp = 64.0f, gLr = 1e-2f;
     int gLobeLoss = 1;
     float sceneLo[3] = {0, 0, 0}, sceneHi[3] = {0, 0, 0};
 
@@ -164,7 +169,7 @@ struct optpt_renderer {
             fp.guide.batch = gBatch;
             fp.guide.batchCount = gBatchCount;
             fp.guide.on = 1;
-            fp.guide.train = guideMode == 1 ? 1u : 0u;
+            fp.guide.train = trainingOpen() ? 1u : 0u;
             fp.guide.trainStride = gTrainStride;
             fp.guide.batchCapacity = gBatchCap;
             fp.guide.step = guide->dStep;
@@ -172,6 +177,7 @@ struct optpt_renderer {
             fp.guide.alphaMax = gAlphaMax;
             fp.guide.alphaRamp = gAlphaRamp;
             fp.guide.maxDepth = gMaxDepth;
+            fp.guide.sharePrimary = gSharePrimary ? 1u : 0u;
         }
         return fp;
     }
@@ -465,6 +471,7 @@ int ensureGraph(optpt_renderer *r, cudaStream_t st)
     r->graphExec = nullptr;
     r->graph = nullptr;
     const FrameParams fp = r->frameParams();
+    r->graphTrain = fp.guide.train != 0;
     CUDA_OR_RETURN(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
     enqueuePass(r, fp, st, nullptr, nullptr);
     cudaError_t e = cudaStreamEndCapture(st, &r->graph);
@@ -1049,6 +1056,7 @@ int optpt_set_guiding(optpt_renderer *r, int mode)
         g->lr = r->gLr;
         g->lobeLoss = r->gLobeLoss;
         r->guide = g;
+        r->gTrainedSpp = 0;
     }
     if (mode != r->guideMode) {
         r->guideMode = mode;
@@ -1080,6 +1088,12 @@ int optpt_set_guiding_options(optpt_renderer *r, const optpt_guiding_options *o)
         r->gTrainStride = o->trainStride;
     if (o->maxDepth)
         r->gMaxDepth = o->maxDepth;
+    if (o->primaryShare)
+        r->gSharePrimary = o->primaryShare > 0;
+    if (o->trainSpp && o->trainSpp != r->gTrainSpp) {
+        r->gTrainSpp = o->trainSpp;
+        r->gTrainedSpp = 0;  // a new budget starts now
+    }
     if (o->alphaMax > 0.0f)
         r->gAlphaMax = o->alphaMax;
     if (o->alphaRamp > 0.0f)
@@ -1100,6 +1114,8 @@ int optpt_get_guiding_options(const optpt_renderer *r, optpt_guiding_options *o)
     o->trainSteps = r->gTrainSteps;
     o->trainStride = r->gTrainStride;
     o->maxDepth = r->gMaxDepth;
+    o->trainSpp = r->gTrainSpp;
+    o->primaryShare = r->gSharePrimary ? 1 : -1;
     o->alphaMin = r->gAlphaMin;
     o->alphaMax = r->gAlphaMax;
     o->lobeLoss = r->gLobeLoss + 1;
@@ -1242,21 +1258,30 @@ int optpt_render(optpt_renderer *r, uint32_t spp, void *stream)
     if ((rc = ensureGuideBuffers(r)))
         return rc;
     const uint32_t passes = spp / r->sppBatch, rem = spp % r->sppBatch;
-    if (r->opt.useGraph && passes) {
-        if ((rc = ensureGraph(r, st ? st : r->ownStream)))
-            return rc;
-        for (uint32_t p = 0; p < passes; ++p)
+    // Online training runs until its sample budget is spent; the pass after
+    // that is recaptured without it (the network is then frozen).
+    for (uint32_t p = 0; p < passes; ++p) {
+        const bool training = r->trainingOpen();
+        if (r->opt.useGraph) {
+            if (training != r->graphTrain)
+                r->graphDirty = true;
+            if ((rc = ensureGraph(r, st ? st : r->ownStream)))
+                return rc;
             CUDA_OR_RETURN(cudaGraphLaunch(r->graphExec, st), "graph launch");
-    } else {
-        const FrameParams fp = r->frameParams();
-        for (uint32_t p = 0; p < passes; ++p)
-            enqueuePass(r, fp, st, nullptr, nullptr);
+        } else {
+            enqueuePass(r, r->frameParams(), st, nullptr, nullptr);
+        }
+        if (training)
+            r->gTrainedSpp += r->sppBatch;
     }
     if (rem) {
+        const bool training = r->trainingOpen();
         FrameParams fp = r->frameParams();
         fp.sppBatch = rem;
         fp.numPaths = r->w * r->h * rem;
         enqueuePass(r, fp, st, nullptr, nullptr);
+        if (training)
+            r->gTrainedSpp += rem;
     }
     CUDA_OR_RETURN(cudaGetLastError(), "kernel launch");
     r->lp.sample += spp;

@@ -79,6 +79,7 @@ struct GuidePass {
     float alphaMax;          // cap on the probability of sampling the learned mixture
     float alphaRamp;         // that probability is min(alphaMax, min(1, steps / alphaRamp) * network's)
     uint32_t maxDepth;       // vertices deeper than this sample the BSDF only
+    uint32_t sharePrimary;   // 1: a pass's first hits of one pixel share one mixture (its first sample's)
 };
 #define GUIDE_REC 7
 

@@ -230,6 +230,8 @@ struct HitInput {
     const float4 *rayO, *rayD, *hit, *triV;
     const uint32_t *countPtr;
     uint32_t n;
+    const uint32_t *limitPtr;  // if set, at most *limitPtr queries (else `limit`, if non-zero)
+    uint32_t limit;
     __device__ bool fetch(uint32_t i, float3 &p, float3 &nrm, float3 &wo) const
     {
         if (i >= n)
@@ -248,7 +250,13 @@ struct HitInput {
         return true;
     }
     __device__ uint32_t count() const { return n; }
-    __device__ void resolve() { n = *countPtr; }
+    __device__ void resolve()
+    {
+        n = *countPtr;
+        const uint32_t cap = limitPtr ? *limitPtr : limit;
+        if (cap && cap < n)
+            n = cap;
+    }
 };
 
 constexpr uint32_t INFER_SMEM = LAYERS * W_BYTES + 2 * TILE_BYTES + 1024;
@@ -319,6 +327,11 @@ __global__ void __launch_bounds__(256, 2)
             Packed pk;
             pack(m, pk);
             out[base + row] = pk;
+        } else if (ok && base + row < n) {
+            // no hit: a null mixture (zero weights, zero selection), so a
+            // vertex that reads this row (a shared primary mixture) samples
+            // the BSDF alone
+            out[base + row] = Packed{};
         }
     }
     if (!ok && row == 0)
@@ -851,7 +864,14 @@ void launchGuideInfer(const optpt_guide *g, const DevScene &sc, const FrameParam
                       cudaStream_t st)
 {
     const int cur = depth & 1;
-    HitInput in{q.rayO[cur], q.rayD[cur], q.hit, sc.triV, q.counters + CNT_EXT + depth, 0u};
+    HitInput in{q.rayO[cur], q.rayD[cur], q.hit, sc.triV, q.counters + CNT_EXT + depth, 0u, nullptr, 0u};
+    if (depth == 1 && fp.guide.sharePrimary) {
+        // one query per pixel: the first sample of each pixel heads the queue
+        if (fp.batch.on)
+            in.limitPtr = fp.batch.dyn;
+        else
+            in.limit = fp.npix;
+    }
     kGuideInfer<HitInput><<<g->numSMs * 2, 256, INFER_SMEM, st>>>(
         guideGeom(g), g->hashH, g->tiles, in, reinterpret_cast<Packed *>(const_cast<void *>(fp.guide.mix)),
         g->status);

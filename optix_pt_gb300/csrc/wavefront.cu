@@ -593,7 +593,12 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
                                 // sampler. The lobe's density decides the kill test, as in
                                 // the plain estimator, so both integrate over the same set.
                                 guide::Mixture gm;
-                                guide::unpack(reinterpret_cast<const guide::Packed *>(gp.mix)[i], gm);
+                                // primary hits of one pixel share its first sample's mixture
+                                const uint32_t mi =
+                                    depth == 1 && gp.sharePrimary
+                                        ? i % (fp.batch.on ? __ldg(fp.batch.dyn) : fp.npix)
+                                        : i;
+                                guide::unpack(reinterpret_cast<const guide::Packed *>(gp.mix)[mi], gm);
                                 // selection probability: the network's, phased in with training
                                 const float alpha =
                                     ramp * fminf(fp.guide.alphaMax, fmaxf(fp.guide.alphaMin, gm.select));

@@ -47,6 +47,8 @@ int main(void) {
   S(Light); S(MaterialData); S(LaunchParams); S(optpt_scene); S(optpt_texture); S(optpt_options);
   S(optpt_stats); S(optpt_kernel_times); S(optpt_bsdf_query); S(optpt_bsdf_result); S(TextureTransform);
   S(optpt_guiding_options); S(optpt_view); S(optpt_autotune_request); S(optpt_autotune_trial);
+  S(optpt_gltf_info_t); S(optpt_deformation); S(optpt_image);
+  O(optpt_deformation, numVertices); O(optpt_guiding_options, trainSpp);
   O(MaterialData, baseColour); O(MaterialData, ior); O(MaterialData, category); O(MaterialData, hasSheenRoughnessTexture);
   O(LaunchParams, traversable); O(LaunchParams, gammaTerm); O(LaunchParams, bgColour);
   O(optpt_scene, camEye); O(optpt_scene, maxDepth); O(optpt_bsdf_query, xs); O(optpt_bsdf_result, pdf);
@@ -74,7 +76,8 @@ def test_struct_layouts_match_c(built):
           "optpt_stats": _ffi.Stats, "optpt_kernel_times": _ffi.KernelTimes,
           "TextureTransform": _ffi.TextureTransform, "optpt_guiding_options": _ffi.GuidingOptions,
           "optpt_view": _ffi.View, "optpt_autotune_request": _ffi.AutotuneRequest,
-          "optpt_autotune_trial": _ffi.AutotuneTrial}
+          "optpt_autotune_trial": _ffi.AutotuneTrial, "optpt_gltf_info_t": _ffi.GltfInfo,
+          "optpt_deformation": _ffi.Deformation, "optpt_image": _ffi.Image}
     for name, cls in py.items():
         assert ctypes.sizeof(cls) == c[name], name
     assert _ffi.BSDF_QUERY.itemsize == c["optpt_bsdf_query"]
@@ -84,6 +87,8 @@ def test_struct_layouts_match_c(built):
     assert _ffi.LaunchParams.traversable.offset == c["LaunchParams.traversable"]
     assert _ffi.LaunchParams.bgColour.offset == c["LaunchParams.bgColour"]
     assert _ffi.SceneStruct.maxDepth.offset == c["optpt_scene.maxDepth"]
+    assert _ffi.Deformation.numVertices.offset == c["optpt_deformation.numVertices"]
+    assert _ffi.GuidingOptions.trainSpp.offset == c["optpt_guiding_options.trainSpp"]
     assert _ffi.BSDF_QUERY.fields["xs"][1] == c["optpt_bsdf_query.xs"]
     assert _ffi.BSDF_RESULT.fields["pdf"][1] == c["optpt_bsdf_result.pdf"]
 
