@@ -25,6 +25,9 @@ struct Bvh8Node {
 };
 
 #define BVH8_STACK 64
+#ifndef TRAV8_REFILL
+#define TRAV8_REFILL 8  // idle lanes that trigger a refill of a persistent warp
+#endif
 
 OPT_D uint32_t byteOf(uint4 v, int k)  // k in 0..15
 {
@@ -38,22 +41,43 @@ OPT_D float byteToFloat(uint32_t w, int k)
     return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)k)) - 8388608.0f;
 }
 
-template <bool ANY, class AlphaFn, class Counter = NoCount>
-OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, float3 o, float3 d,
-                     float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &&ctr = Counter())
-{
-    hit.leaf = -1;
-    if (nodes == nullptr)
-        return false;
-    const RayPre pre = rayPrepare(o, d);
-    const float3 inv = mk3(safeInv(d.x), safeInv(d.y), safeInv(d.z));
-    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+// Traversal state of one ray: registers, plus the node-group stack in local
+// memory. `step` visits one node (and the triangles of the leaf children the
+// ray reaches) and reports whether the ray is finished.
+struct Trav8 {
+    RayPre pre;
+    float3 o, inv;
+    float tmin, tcur;
+    uint32_t oct;
+    int node, sp, bestPrim, budget;
+    // The group the next node comes from (child base, hits << 8 | imask)
+    // stays in registers; a group goes to the stack only when a newer one
+    // replaces it with hits left, and comes back when the newer runs out.
+    uint2 grp;
     uint2 stack[BVH8_STACK];
-    int sp = 0;
-    int node = 0;
-    float tcur = tmax;
-    int bestPrim = INT_MAX;
-    for (int budget = 1 << 24; budget > 0; --budget) {
+
+    OPT_D void init(float3 ro, float3 d, float rtmin, float rtmax, HitRec &hit)
+    {
+        hit.leaf = -1;
+        pre = rayPrepare(ro, d);
+        o = ro;
+        inv = mk3(safeInv(d.x), safeInv(d.y), safeInv(d.z));
+        oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+        tmin = rtmin;
+        tcur = rtmax;
+        node = 0;
+        sp = 0;
+        bestPrim = INT_MAX;
+        budget = 1 << 24;
+        grp = make_uint2(0u, 0u);
+    }
+
+    template <bool ANY, class AlphaFn, class Counter>
+    OPT_D bool step(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, HitRec &hit, AlphaFn &alpha,
+                    Counter &ctr)
+    {
+        if (--budget < 0)
+            return true;
         ctr.node();
         const Bvh8Node *N = nodes + node;
         const float4 a = __ldg(&N->a);
@@ -114,7 +138,7 @@ OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restric
                     hit.u = u;
                     hit.v = v;
                     hit.leaf = k;
-                    return true;
+                    return true;  // occluded: finished
                 }
                 if (t < tcur || prim < bestPrim) {
                     tcur = t;
@@ -126,22 +150,89 @@ OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restric
                 }
             }
         }
-        if (ihits && sp < BVH8_STACK)
-            stack[sp++] = make_uint2(b.x, (ihits << 8) | imask);
-        if (sp == 0)
-            break;
-        // Next internal child: lowest set bit of the top group (octant order).
-        uint2 &g = stack[sp - 1];
-        uint32_t hits = g.y >> 8;
-        const uint32_t gmask = g.y & 0xFFu;
+        if (ihits) {
+            if ((grp.y >> 8) && sp < BVH8_STACK)
+                stack[sp++] = grp;
+            grp = make_uint2(b.x, (ihits << 8) | imask);
+        }
+        if (!(grp.y >> 8)) {
+            if (sp == 0)
+                return true;  // nothing left to visit
+            grp = stack[--sp];
+        }
+        // Next internal child: lowest set bit of the current group (octant order).
+        uint32_t hits = grp.y >> 8;
+        const uint32_t gmask = grp.y & 0xFFu;
         const uint32_t bpos = (uint32_t)(__ffs(hits) - 1);
         const uint32_t s = bpos ^ oct;
         hits &= hits - 1u;
-        node = (int)g.x + __popc(gmask & ((1u << s) - 1u));
-        if (hits)
-            g.y = (hits << 8) | gmask;
-        else
-            --sp;
+        node = (int)grp.x + __popc(gmask & ((1u << s) - 1u));
+        grp.y = (hits << 8) | gmask;
+        return false;
+    }
+};
+
+template <bool ANY, class AlphaFn, class Counter = NoCount>
+OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, float3 o, float3 d,
+                     float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &&ctr = Counter())
+{
+    hit.leaf = -1;
+    if (nodes == nullptr)
+        return false;
+    Trav8 T;
+    T.init(o, d, tmin, tmax, hit);
+    while (!T.step<ANY>(nodes, triV, hit, alpha, ctr)) {
     }
     return hit.leaf >= 0;
+}
+
+// A queue of rays traversed by persistent warps with lane refill (dynamic
+// ray fetch, after Aila and Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", HPG 2009): a lane whose ray is finished takes the next
+// ray of the queue (one atomicAdd per warp for all lanes needing one), so no
+// lane idles while the longest ray of its warp finishes. Every lane runs the
+// same per-ray traversal as traverse8. All 32 lanes of each warp must call
+// it. fetch(i, o, d, tmin, tmax, alpha) loads ray i (and its alpha-test
+// parameters); finish(i, hit) stores ray i's result.
+template <bool ANY, class Fetch, class Finish, class AlphaFn, class Counter>
+OPT_D void traverse8Queue(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, uint32_t count,
+                          uint32_t *next, Fetch fetch, Finish finish, AlphaFn alpha, Counter &ctr)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    Trav8 T;
+    HitRec hit;
+    hit.leaf = -1;
+    int ray = -1;
+    bool exhausted = false;
+    while (true) {
+        const bool need = ray < 0 && !exhausted;
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        // Refill in batches: a fetch stalls the whole warp on the atomic, so
+        // wait until enough lanes are idle (or none is busy).
+        if (nm && (__popc(nm) >= TRAV8_REFILL || __ballot_sync(0xffffffffu, ray >= 0) == 0u)) {
+            const int leader = __ffs(nm) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader)
+                base = atomicAdd(next, (uint32_t)__popc(nm));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const uint32_t i = base + (uint32_t)__popc(nm & ((1u << lane) - 1u));
+                if (i < count) {
+                    float3 o, d;
+                    float tmin, tmax;
+                    fetch(i, o, d, tmin, tmax, alpha);
+                    T.init(o, d, tmin, tmax, hit);
+                    ray = (int)i;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray >= 0) == 0u)
+            break;
+        if (ray >= 0 && (nodes == nullptr || T.step<ANY>(nodes, triV, hit, alpha, ctr))) {
+            finish((uint32_t)ray, hit);
+            ray = -1;
+        }
+    }
 }

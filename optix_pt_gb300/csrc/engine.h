@@ -148,7 +148,9 @@ __device__ __forceinline__ uint32_t passPaths(const FrameParams &fp)
 #define CNT_EXT 0
 #define CNT_SHADOW_P 64
 #define CNT_SHADOW_E 128
-#define CNT_TOTAL 192
+// next unclaimed ray of each extension queue (persistent warps with lane refill)
+#define CNT_FETCH_EXT 192
+#define CNT_TOTAL 256
 #define OPT_MAX_DEPTH 62
 
 // Wavefront buffers (SoA; P = numPaths):

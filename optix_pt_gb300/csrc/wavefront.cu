@@ -232,16 +232,34 @@ __global__ void __launch_bounds__(256, OPTPT_TRAV_MINB) kExtend(DevScene s, Fram
     const uint32_t sampleBase = __ldg(fp.state);
     const uint32_t seed = __float_as_uint(__ldg(&fp.fc->eye).w);
     typename std::conditional<COUNT, Count, NoCount>::type ctr;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
-        const float4 ro = q.rayO[cur][i], rd = q.rayD[cur][i];
-        const uint32_t path = (uint32_t)__float_as_int(ro.w);
-        uint32_t pixel, sample;
-        pathPixelSample(fp, path, pixel, sample);
-        const AlphaTest at = makeAlpha(s, seed, pixel, sample, (uint32_t)depth, -1.0f);
-        HitRec h;
-        const bool hit = traceScene<false, WIDE>(s, f3of4(ro), f3of4(rd), 0.0f, 1e16f, h, at, ctr);
-        q.hit[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.leaf))
-                       : make_float4(__int_as_float(0x7f800000), 0.0f, 0.0f, __int_as_float(-1));
+    if constexpr (WIDE) {
+        // persistent warps over the queue, lanes refilled as their rays finish
+        auto fetch = [&](uint32_t i, float3 &o, float3 &d, float &tmin, float &tmax, AlphaTest &at) {
+            const float4 ro = q.rayO[cur][i], rd = q.rayD[cur][i];
+            pathPixelSample(fp, (uint32_t)__float_as_int(ro.w), at.pixel, at.sample);
+            o = f3of4(ro);
+            d = f3of4(rd);
+            tmin = 0.0f;
+            tmax = 1e16f;
+        };
+        auto finish = [&](uint32_t i, const HitRec &h) {
+            q.hit[i] = h.leaf >= 0 ? make_float4(h.t, h.u, h.v, __int_as_float(h.leaf))
+                                   : make_float4(__int_as_float(0x7f800000), 0.0f, 0.0f, __int_as_float(-1));
+        };
+        traverse8Queue<false>(s.nodes8, s.triV, count, q.counters + CNT_FETCH_EXT + depth, fetch, finish,
+                              makeAlpha(s, seed, 0u, 0u, (uint32_t)depth, -1.0f), ctr);
+    } else {
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+            const float4 ro = q.rayO[cur][i], rd = q.rayD[cur][i];
+            const uint32_t path = (uint32_t)__float_as_int(ro.w);
+            uint32_t pixel, sample;
+            pathPixelSample(fp, path, pixel, sample);
+            const AlphaTest at = makeAlpha(s, seed, pixel, sample, (uint32_t)depth, -1.0f);
+            HitRec h;
+            const bool hit = traceScene<false, WIDE>(s, f3of4(ro), f3of4(rd), 0.0f, 1e16f, h, at, ctr);
+            q.hit[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.leaf))
+                           : make_float4(__int_as_float(0x7f800000), 0.0f, 0.0f, __int_as_float(-1));
+        }
     }
     if constexpr (COUNT)
         flushCounts(ctr, q.totals, 4);
@@ -692,6 +710,19 @@ __global__ void __launch_bounds__(256, OPTPT_TRAV_MINB)
     const uint32_t sampleBase = __ldg(fp.state);
     const uint32_t seed = __float_as_uint(__ldg(&fp.fc->eye).w);
     typename std::conditional<COUNT, Count, NoCount>::type ctr;
+    // An unoccluded ray adds its contribution; an occluded one adds c * 0.
+    auto resolve = [&](uint32_t path, float4 c, bool occluded) {
+        const float3 cc = f3of4(c);
+        const bool finite = isfinite(cc.x) && isfinite(cc.y) && isfinite(cc.z);
+        if (!occluded || !finite) {
+            float4 L = q.pathL[path];
+            const float3 add = occluded ? cc * 0.0f : cc;
+            q.pathL[path] = make_float4(L.x + add.x, L.y + add.y, L.z + add.z, L.w);
+        }
+    };
+    // Shadow rays are short: a lane-refilling persistent warp (as the
+    // extension kernel uses) spends more on refills than it saves here
+    // (measured), so each thread walks the queue with a fixed stride.
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
         const float4 o = q.shO[which][j], d = q.shD[which][j], c = q.shC[which][j];
         const uint32_t path = (uint32_t)__float_as_int(o.w);
@@ -701,13 +732,7 @@ __global__ void __launch_bounds__(256, OPTPT_TRAV_MINB)
         HitRec h;
         const bool occluded =
             traceScene<true, WIDE>(s, f3of4(o), f3of4(d), OPT_SCENE_EPSILON, d.w, h, at, ctr);
-        const float3 cc = f3of4(c);
-        const bool finite = isfinite(cc.x) && isfinite(cc.y) && isfinite(cc.z);
-        if (!occluded || !finite) {
-            float4 L = q.pathL[path];
-            const float3 add = occluded ? cc * 0.0f : cc;
-            q.pathL[path] = make_float4(L.x + add.x, L.y + add.y, L.z + add.z, L.w);
-        }
+        resolve(path, c, occluded);
     }
     if constexpr (COUNT)
         flushCounts(ctr, q.totals, 6);
