@@ -98,10 +98,11 @@ struct Trav8 {
         const float tlim = tcur * BOX_WIDEN;
         uint32_t ihits = 0, lhits = 0;
 #pragma unroll
+        // Empty slots are not skipped: their boxes are the single point at the
+        // node's origin (all-zero quantised bounds), which a ray reaches only
+        // by grazing that point, and then the slot counts as a leaf of zero
+        // triangles. Testing all eight saves the per-slot branch.
         for (int s = 0; s < 8; ++s) {
-            const uint32_t meta = byteOf(b, 8 + s);
-            if (meta == 0u)
-                continue;
             const int k = s & 3;
             const float xn = fmaf(byteToFloat(s < 4 ? nx0 : nx1, k), axs, bx);
             const float xf = fmaf(byteToFloat(s < 4 ? fx0 : fx1, k), axs, bx);
