@@ -112,7 +112,8 @@ int optpt_scene_from_config(const char *sceneListPath, optpt_scene *out);
  * flattened to world space, materials with KHR_materials_{specular,
  * transmission, ior, emissive_strength, clearcoat, sheen} and
  * KHR_texture_transform, PNG textures decoded to RGBA8, KHR_lights_punctual
- * lights and the first perspective camera. upHint may be NULL ((0, 1, 0)).
+ * lights and the first perspective camera; PNG and baseline JPEG images.
+ * upHint may be NULL ((0, 1, 0)).
  * Frame defaults: 1280 x 720, 64 spp, depth 8. Errors: OPTPT_ERR_IO for an
  * unreadable file, OPTPT_ERR_PARSE for malformed JSON, buffers or images. */
 int optpt_scene_from_gltf(const char *path, const float upHint[3], optpt_scene *out);
@@ -181,6 +182,10 @@ typedef struct optpt_image {
  * tRNS apply, Adam7 interlacing is undone. OPTPT_ERR_PARSE on a malformed or
  * truncated file (CRC and Adler-32 checked). */
 int optpt_image_decode_png(const void *data, size_t size, optpt_image *out);
+/* Decodes a baseline or extended-sequential JPEG (Huffman, 8-bit; grey,
+ * YCbCr with any chroma subsampling, Adobe RGB; restart intervals) to RGBA8
+ * with alpha 255. Progressive and arithmetic-coded files: OPTPT_ERR_PARSE. */
+int optpt_image_decode_jpeg(const void *data, size_t size, optpt_image *out);
 void optpt_image_release(optpt_image *img);
 
 /* ------------------------------------------------------------------ renderer */

@@ -15,7 +15,7 @@ import numpy as np
 from . import _ffi
 from ._ffi import BSDF_QUERY, BSDF_RESULT, OptptError, check, lib
 
-__all__ = ["Scene", "SceneDesc", "GltfModel", "Animator", "decode_png", "encode_png", "encode_hdr", "encode_exr", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
+__all__ = ["Scene", "SceneDesc", "GltfModel", "Animator", "decode_png", "decode_jpeg", "encode_png", "encode_hdr", "encode_exr", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
            "library_path"]
 
 library_path = _ffi.LIB_PATH
@@ -113,16 +113,25 @@ class Scene:
         return out
 
 
-def decode_png(data):
-    """Decodes PNG bytes to an HxWx4 uint8 array with the library's decoder."""
+def _decode(fn, data):
     img = _ffi.Image()
     buf = ctypes.create_string_buffer(bytes(data), len(data))
-    check(lib.optpt_image_decode_png(buf, len(data), ctypes.byref(img)))
+    check(fn(buf, len(data), ctypes.byref(img)))
     try:
         return np.ctypeslib.as_array(img.rgba, shape=(img.height * img.width * 4,)).copy().reshape(
             img.height, img.width, 4)
     finally:
         lib.optpt_image_release(ctypes.byref(img))
+
+
+def decode_png(data):
+    """Decodes PNG bytes to an HxWx4 uint8 array with the library's decoder."""
+    return _decode(lib.optpt_image_decode_png, data)
+
+
+def decode_jpeg(data):
+    """Decodes baseline JPEG bytes to an HxWx4 uint8 array with the library's decoder."""
+    return _decode(lib.optpt_image_decode_jpeg, data)
 
 
 class GltfModel:

@@ -176,6 +176,7 @@ _sigs = {
     "optpt_scene_from_config": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(SceneStruct)]),
     "optpt_scene_from_gltf": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.POINTER(SceneStruct)]),
     "optpt_image_decode_png": (ctypes.c_int, [_P, ctypes.c_size_t, ctypes.POINTER(Image)]),
+    "optpt_image_decode_jpeg": (ctypes.c_int, [_P, ctypes.c_size_t, ctypes.POINTER(Image)]),
     "optpt_image_release": (None, [ctypes.POINTER(Image)]),
     "optpt_gltf_open": (ctypes.c_int, [ctypes.c_char_p, _P, ctypes.POINTER(_P)]),
     "optpt_gltf_close": (None, [_P]),

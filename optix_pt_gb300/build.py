@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(ROOT, "_build", "optpt")
 LIB = os.path.join(OUT_DIR, "liboptpt.so")
 
 CUDA_SOURCES = ["bvh_build.cu", "bvh8_build.cu", "wavefront.cu", "engine.cu", "metrics.cu", "guide.cu", "image_out.cu", "deform.cu"]
-CXX_SOURCES = ["scenes.cpp", "autotune.cpp", "gltf.cpp", "image_io.cpp", "image_encode.cpp"]
+CXX_SOURCES = ["scenes.cpp", "autotune.cpp", "gltf.cpp", "image_io.cpp", "image_encode.cpp", "jpeg.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -17,7 +17,7 @@
 //   sheenColorFactor is present and sheen roughness only when
 //   sheenRoughnessFactor is; texture transforms carry offset, rotation and
 //   scale and every texture reads TEXCOORD_0;
-// * textures as RGBA8 (stb's four-component decode): the base-colour
+// * textures (PNG, baseline JPEG) as RGBA8 (stb's four-component decode): the base-colour
 //   texture takes its sampler's wrap modes and magnification filter, the
 //   others repeat and filter linearly (src/renderer.cpp:1439-1757); base
 //   colour, emissive and both sheen textures decode sRGB;
@@ -536,11 +536,14 @@ struct Loader {
             }
             optimg::Image decoded;
             std::string e;
-            if (!optimg::isPng(bytes.data(), bytes.size())) {
-                d.err.set(OPTPT_ERR_PARSE, "image " + std::to_string(img) + ": only PNG images are supported");
+            const bool png = optimg::isPng(bytes.data(), bytes.size());
+            const bool jpeg = !png && optimg::isJpeg(bytes.data(), bytes.size());
+            if (!png && !jpeg) {
+                d.err.set(OPTPT_ERR_PARSE, "image " + std::to_string(img) + ": only PNG and JPEG images are supported");
                 return -2;
             }
-            if (!optimg::decodePng(bytes.data(), bytes.size(), decoded, e)) {
+            if (!(png ? optimg::decodePng(bytes.data(), bytes.size(), decoded, e)
+                      : optimg::decodeJpeg(bytes.data(), bytes.size(), decoded, e))) {
                 d.err.set(OPTPT_ERR_PARSE, "image " + std::to_string(img) + ": " + e);
                 return -2;
             }
@@ -1603,7 +1606,6 @@ int optpt_gltf_apply(const optpt_gltf *g, float time, float *positions, float *n
 }
 
 int optpt_image_decode_png(const void *data, size_t size, optpt_image *out)
-
 {
     if (!data || !out)
         return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
@@ -1612,6 +1614,25 @@ int optpt_image_decode_png(const void *data, size_t size, optpt_image *out)
     std::string e;
     if (!optimg::decodePng((const uint8_t *)data, size, img, e))
         return optpt_internal_set_error(OPTPT_ERR_PARSE, ("PNG: " + e).c_str());
+    uint8_t *px = (uint8_t *)malloc(img.rgba.size());
+    if (!px)
+        return optpt_internal_set_error(OPTPT_ERR_NOMEM, "image allocation failed");
+    memcpy(px, img.rgba.data(), img.rgba.size());
+    out->width = img.width;
+    out->height = img.height;
+    out->rgba = px;
+    return OPTPT_OK;
+}
+
+int optpt_image_decode_jpeg(const void *data, size_t size, optpt_image *out)
+{
+    if (!data || !out)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    memset(out, 0, sizeof(*out));
+    optimg::Image img;
+    std::string e;
+    if (!optimg::decodeJpeg((const uint8_t *)data, size, img, e))
+        return optpt_internal_set_error(OPTPT_ERR_PARSE, ("JPEG: " + e).c_str());
     uint8_t *px = (uint8_t *)malloc(img.rgba.size());
     if (!px)
         return optpt_internal_set_error(OPTPT_ERR_NOMEM, "image allocation failed");

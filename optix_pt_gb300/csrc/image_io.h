@@ -32,6 +32,13 @@ bool isPng(const uint8_t *p, size_t n);
 // high byte, low bit depths scale to 0..255, palette and tRNS apply.
 bool decodePng(const uint8_t *p, size_t n, Image &img, std::string &err);
 
+bool isJpeg(const uint8_t *p, size_t n);
+// Decodes a baseline / extended-sequential (Huffman, 8-bit) JPEG to RGBA8
+// (alpha 255): grey, YCbCr with any sampling factors (chroma upsampled by
+// centred bilinear interpolation) or Adobe RGB; restart intervals and
+// multi-scan frames. Progressive and arithmetic-coded files are errors.
+bool decodeJpeg(const uint8_t *p, size_t n, Image &img, std::string &err);
+
 // ---------------------------------------------------------------- encoders
 // DEFLATE with dynamic Huffman codes (greedy LZ77 over a 32 KB window, hash
 // chains; a block falls back to stored when that is smaller). `sync` ends

@@ -3,6 +3,11 @@
 * PNG: every colour type and bit depth, palettes and tRNS, Adam7, all five
   row filters and every DEFLATE block type decode exactly to the four-
   component RGBA8 stb_image gives; corrupt files are errors.
+* JPEG (baseline): grey and YCbCr with 4:4:4, 4:2:2, 4:4:0, 4:2:0 and 4:1:1
+  sampling, Adobe RGB, restart intervals, one scan per component, 16-bit
+  quantisation tables, sizes that are not whole blocks, decode within one
+  level of a float64 reconstruction of the encoder's coefficients
+  (tests/jpeg_writer.py); progressive files are reported as unsupported.
 * glTF: a procedural scene exported to glTF (.gltf with a data-URI buffer,
   external .bin, and .glb) imports to the identical flattened arrays; node
   transforms (matrix and T*R*S, nested), normals through the inverse
@@ -374,10 +379,67 @@ def test_gltf_errors(tmp_path):
     jpg = g.image(b"\xff\xd8\xff\xe0" + b"\0" * 64, mime="image/jpeg")
     m = g.material(pbrMetallicRoughness={"baseColorTexture": {"index": g.texture(jpg)}})
     g.node(mesh=g.mesh([g.primitive(tri, material=m)]))
-    with pytest.raises(opt.OptptError, match="PNG"):
-        opt.Scene.from_gltf(g.save(tmp_path / "jpg.gltf"))
+    with pytest.raises(opt.OptptError, match="JPEG"):
+        opt.Scene.from_gltf(g.save(tmp_path / "badjpg.gltf"))
+    g = Gltf()
+    gif = g.image(b"GIF89a" + b"\0" * 64, mime="image/gif")
+    m = g.material(pbrMetallicRoughness={"baseColorTexture": {"index": g.texture(gif)}})
+    g.node(mesh=g.mesh([g.primitive(tri, material=m)]))
+    with pytest.raises(opt.OptptError, match="only PNG and JPEG"):
+        opt.Scene.from_gltf(g.save(tmp_path / "gif.gltf"))
     g = Gltf()
     g.node(mesh=g.mesh([g.primitive(tri)]))
     g.doc["asset"]["version"] = "1.0"
     with pytest.raises(opt.OptptError, match="version"):
         opt.Scene.from_gltf(g.save(tmp_path / "v1.gltf"))
+
+
+def _jpeg_image(h, w, grey, seed):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w]
+    base = np.stack([(x * 3) % 256, (y * 2 + x) % 256, 128 + 60 * np.sin(x / 7.0) * np.cos(y / 5.0)], -1)
+    a = np.clip(base + rng.normal(0, 6, base.shape), 0, 255).astype(np.uint8)
+    return a[..., 0] if grey else a
+
+
+JPEG_CASES = [dict(hs=1, vs=1), dict(hs=2, vs=2), dict(hs=2, vs=1), dict(hs=1, vs=2), dict(hs=4, vs=1),
+              dict(hs=2, vs=2, restart=3), dict(hs=2, vs=2, separate_scans=True), dict(hs=1, vs=1, q16=True),
+              dict(hs=1, vs=1, adobe_rgb=True)]
+
+
+@pytest.mark.parametrize("case", range(len(JPEG_CASES)))
+@pytest.mark.parametrize("h,w", [(37, 53), (16, 16), (1, 1), (70, 33)])
+def test_jpeg_decodes_within_one_level(case, h, w):
+    from jpeg_writer import encode_jpeg, reconstruct
+    b, info = encode_jpeg(_jpeg_image(h, w, False, case), quality=80, seed=case, **JPEG_CASES[case])
+    d = np.abs(opt.decode_jpeg(b).astype(int) - reconstruct(info).astype(int))
+    assert d.max() <= 1 and (h * w < 256 or d.mean() < 0.05), (d.max(), d.mean())
+
+
+def test_jpeg_grey_and_errors():
+    from jpeg_writer import encode_jpeg, reconstruct
+    b, info = encode_jpeg(_jpeg_image(29, 41, True, 1), quality=50, restart=2)
+    d = np.abs(opt.decode_jpeg(b).astype(int) - reconstruct(info).astype(int))
+    assert d.max() <= 1
+    progressive = bytearray(b)
+    i = progressive.index(b"\xff\xc0")
+    progressive[i + 1] = 0xC2
+    with pytest.raises(opt.OptptError, match="progressive"):
+        opt.decode_jpeg(bytes(progressive))
+    for bad in (b[: len(b) // 3], b"\xff\xd8\xff\xd9", b"\x00\x01"):
+        with pytest.raises(opt.OptptError):
+            opt.decode_jpeg(bad)
+
+
+def test_gltf_with_jpeg_texture(tmp_path):
+    from jpeg_writer import encode_jpeg, reconstruct
+    b, info = encode_jpeg(_jpeg_image(24, 40, False, 3), quality=90, hs=2, vs=2)
+    g = Gltf()
+    m = g.material(pbrMetallicRoughness={"baseColorTexture": {"index": g.texture(g.image(b, mime="image/jpeg"))}})
+    g.node(mesh=g.mesh([g.primitive(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32),
+                                    texcoords=[[0, 0], [1, 0], [0, 1]], material=m)]))
+    sc = opt.Scene.from_gltf(g.save(tmp_path / "j.glb", glb=True))
+    tex = sc.textures()
+    assert len(tex) == 1 and tex[0]["srgb"] == 1
+    d = np.abs(tex[0]["rgba"].astype(int) - reconstruct(info).astype(int))
+    assert d.max() <= 1
