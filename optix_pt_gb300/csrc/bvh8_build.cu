@@ -89,16 +89,29 @@ __global__ void kCollapseOpen(const BvhNode *__restrict__ n2, const int *__restr
     nTri[i] = t;
 }
 
-OPT_D int scaleExponent(double ext)  // smallest e with 253 * 2^e >= ext, in [-126, 127]
+// Box quantisation shared by the collapse and the refit, in FP32 with
+// directed rounding so that it is cheap on the GPU and still conservative:
+// the extent is rounded up, a child's offset from the node origin rounded
+// down (low bound) or up (high bound), then widened by one step.
+OPT_D int scaleExponent(float ext)  // smallest e with 253 * 2^e >= ext, in [-126, 127]
 {
-    if (!(ext > 0.0))
+    if (!(ext > 0.0f))
         return -126;
-    int e = ilogb(ext) - 7;
-    while (ldexp(253.0, e) < ext)
+    int e = ilogbf(ext) - 7;
+    while (ldexpf(253.0f, e) < ext)
         ++e;
-    while (e > -126 && ldexp(253.0, e - 1) >= ext)
+    while (e > -126 && ldexpf(253.0f, e - 1) >= ext)
         --e;
     return max(-126, min(127, e));
+}
+OPT_D void quantise(float elo, float ehi, float lo, int ex, uint32_t &ql, uint32_t &qh)
+{
+    const float inv = ldexpf(1.0f, -ex);
+    float a = floorf(__fsub_rd(elo, lo) * inv), b = ceilf(__fsub_ru(ehi, lo) * inv);
+    a = a > 0.0f ? a - 1.0f : 0.0f;
+    b = fminf(b + 1.0f, 255.0f);
+    ql = (uint32_t)a;
+    qh = (uint32_t)fmaxf(b, 0.0f);
 }
 
 __global__ void kCollapseEmit(const int *__restrict__ items, int nItems, const Entry *__restrict__ ent,
@@ -154,7 +167,7 @@ __global__ void kCollapseEmit(const int *__restrict__ items, int nItems, const E
     }
     int ex[3];
     for (int k = 0; k < 3; ++k)
-        ex[k] = scaleExponent((double)hi[k] - (double)lo[k]);
+        ex[k] = scaleExponent(__fsub_ru(hi[k], lo[k]));
     uint32_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0}, qlo[3][8], qhi[3][8];
     int refAt[8];
     for (int s = 0; s < 8; ++s) {
@@ -172,15 +185,8 @@ __global__ void kCollapseEmit(const int *__restrict__ items, int nItems, const E
         const int j = refAt[s];
         if (j < 0)
             continue;
-        for (int k = 0; k < 3; ++k) {
-            const double inv = ldexp(1.0, -ex[k]);
-            double ql = floor(((double)e[j].lo[k] - (double)lo[k]) * inv);
-            double qh = ceil(((double)e[j].hi[k] - (double)lo[k]) * inv);
-            ql = ql > 0.0 ? ql - 1.0 : 0.0;
-            qh = fmin(qh + 1.0, 255.0);
-            qlo[k][s] = (uint32_t)ql;
-            qhi[k][s] = (uint32_t)qh;
-        }
+        for (int k = 0; k < 3; ++k)
+            quantise(e[j].lo[k], e[j].hi[k], lo[k], ex[k], qlo[k][s], qhi[k][s]);
         if (e[j].cnt == 0) {
             imask |= 1u << s;
             meta[s] = 1u;
@@ -235,89 +241,96 @@ __global__ void kRefitTris(int n, const float *__restrict__ pos, const int *__re
     }
 }
 
-// Refit, step 2 (one launch per level, deepest first): each node's child
-// boxes from its internal children's refit boxes and its leaf triangles,
-// its frame and quantised boxes recomputed exactly as kCollapseEmit does.
+// Refit, step 2 (one launch per level, deepest first): eight lanes per node,
+// one per child slot. A lane forms its slot's box (an internal child's refit
+// box, or its leaf triangles' bounds); the node box is the union over the
+// eight lanes (shuffles); each lane quantises its own slot exactly as the
+// collapse does, and the bytes are packed into the node's words by shuffles.
 // With unchanged vertices the nodes come out bit-identical.
-__global__ void kRefitLevel(int begin, int end, Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV8,
-                            float *__restrict__ box8, int numNodes8, int numTris)
+__global__ void __launch_bounds__(128) kRefitLevel(int begin, int end, Bvh8Node *__restrict__ nodes,
+                                                   const float4 *__restrict__ triV8, float *__restrict__ box8,
+                                                   int numNodes8, int numTris)
 {
-    const int i = begin + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (i >= end)
-        return;
-    Bvh8Node N = nodes[i];
-    const uint32_t ew = __float_as_uint(N.a.w), imask = ew >> 24;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = begin + (t >> 3), s = t & 7;
+    const bool live = i < end;
     const float inf = __int_as_float(0x7f800000);
-    float elo[8][3], ehi[8][3];
-    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-    uint32_t present = 0;
-    for (int s = 0; s < 8; ++s) {
-        const uint32_t meta = byteOf(N.b, 8 + s);
-        for (int k = 0; k < 3; ++k) {
-            elo[s][k] = inf;
-            ehi[s][k] = -inf;
-        }
-        if (meta == 0u)
-            continue;
-        present |= 1u << s;
-        if ((imask >> s) & 1u) {
-            const int c = (int)N.b.x + __popc(imask & ((1u << s) - 1u));
-            if (c < 0 || c >= numNodes8)
-                continue;
-            for (int k = 0; k < 3; ++k) {
-                elo[s][k] = box8[6 * (size_t)c + k];
-                ehi[s][k] = box8[6 * (size_t)c + 3 + k];
-            }
-        } else {
-            const int first = (int)N.b.y + (int)(meta & 31u), cnt = (int)(meta >> 5);
-            for (int t = first; t < first + cnt && t < numTris; ++t)
+    float elo[3] = {inf, inf, inf}, ehi[3] = {-inf, -inf, -inf};
+    uint4 b = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t imask = 0;
+    bool present = false;
+    if (live) {
+        b = nodes[i].b;
+        imask = __float_as_uint(nodes[i].a.w) >> 24;
+        const uint32_t meta = byteOf(b, 8 + s);
+        present = meta != 0u;
+        if (present && ((imask >> s) & 1u)) {
+            const int c = (int)b.x + __popc(imask & ((1u << s) - 1u));
+            if (c >= 0 && c < numNodes8)
+                for (int k = 0; k < 3; ++k) {
+                    elo[k] = box8[6 * (size_t)c + k];
+                    ehi[k] = box8[6 * (size_t)c + 3 + k];
+                }
+        } else if (present) {
+            const int first = (int)b.y + (int)(meta & 31u), cnt = (int)(meta >> 5);
+            for (int tr = first; tr < first + cnt && tr < numTris; ++tr)
                 for (int v = 0; v < 3; ++v) {
-                    const float4 p = triV8[3 * (size_t)t + v];
-                    elo[s][0] = fminf(elo[s][0], p.x);
-                    elo[s][1] = fminf(elo[s][1], p.y);
-                    elo[s][2] = fminf(elo[s][2], p.z);
-                    ehi[s][0] = fmaxf(ehi[s][0], p.x);
-                    ehi[s][1] = fmaxf(ehi[s][1], p.y);
-                    ehi[s][2] = fmaxf(ehi[s][2], p.z);
+                    const float4 p = triV8[3 * (size_t)tr + v];
+                    elo[0] = fminf(elo[0], p.x);
+                    elo[1] = fminf(elo[1], p.y);
+                    elo[2] = fminf(elo[2], p.z);
+                    ehi[0] = fmaxf(ehi[0], p.x);
+                    ehi[1] = fmaxf(ehi[1], p.y);
+                    ehi[2] = fmaxf(ehi[2], p.z);
                 }
         }
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = fminf(lo[k], elo[s][k]);
-            hi[k] = fmaxf(hi[k], ehi[s][k]);
+    }
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = elo[k];
+        hi[k] = ehi[k];
+        for (int off = 1; off < 8; off <<= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], off));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], off));
         }
     }
     int ex[3];
-    for (int k = 0; k < 3; ++k)
-        ex[k] = scaleExponent((double)hi[k] - (double)lo[k]);
-    uint32_t qlo[3][8], qhi[3][8];
-    for (int s = 0; s < 8; ++s) {
-        for (int k = 0; k < 3; ++k) {
-            qlo[k][s] = qhi[k][s] = 0u;
-            if (!((present >> s) & 1u))
-                continue;
-            const double inv = ldexp(1.0, -ex[k]);
-            double ql = floor(((double)elo[s][k] - (double)lo[k]) * inv);
-            double qh = ceil(((double)ehi[s][k] - (double)lo[k]) * inv);
-            ql = ql > 0.0 ? ql - 1.0 : 0.0;
-            qh = fmin(qh + 1.0, 255.0);
-            qlo[k][s] = (uint32_t)ql;
-            qhi[k][s] = (uint32_t)qh;
+    uint32_t ql[3] = {0u, 0u, 0u}, qh[3] = {0u, 0u, 0u};
+    for (int k = 0; k < 3; ++k) {
+        ex[k] = scaleExponent(__fsub_ru(hi[k], lo[k]));
+        if (present)
+            quantise(elo[k], ehi[k], lo[k], ex[k], ql[k], qh[k]);
+    }
+    // pack: word of slots 0-3 (or 4-7) from the lanes of this quad
+    const int sh = 8 * (s & 3);
+    uint32_t wl[3], wh[3];
+    for (int k = 0; k < 3; ++k) {
+        wl[k] = ql[k] << sh;
+        wh[k] = qh[k] << sh;
+        for (int off = 1; off < 4; off <<= 1) {
+            wl[k] |= __shfl_xor_sync(0xffffffffu, wl[k], off);
+            wh[k] |= __shfl_xor_sync(0xffffffffu, wh[k], off);
         }
     }
-    const uint32_t nw = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) | ((uint32_t)(ex[2] + 127) << 16) |
-                        (imask << 24);
-    N.a = make_float4(lo[0], lo[1], lo[2], __uint_as_float(nw));
-    uint4 *q[3] = {&N.qx, &N.qy, &N.qz};
-    for (int k = 0; k < 3; ++k) {
-        q[k]->x = qlo[k][0] | qlo[k][1] << 8 | qlo[k][2] << 16 | qlo[k][3] << 24;
-        q[k]->y = qlo[k][4] | qlo[k][5] << 8 | qlo[k][6] << 16 | qlo[k][7] << 24;
-        q[k]->z = qhi[k][0] | qhi[k][1] << 8 | qhi[k][2] << 16 | qhi[k][3] << 24;
-        q[k]->w = qhi[k][4] | qhi[k][5] << 8 | qhi[k][6] << 16 | qhi[k][7] << 24;
+    if (!live)
+        return;
+    Bvh8Node *N = nodes + i;
+    uint32_t *qw[3] = {&N->qx.x, &N->qy.x, &N->qz.x};
+    if (s == 0 || s == 4) {
+        const int half = s >> 2;  // 0: slots 0-3 (words x, z), 1: slots 4-7 (words y, w)
+        for (int k = 0; k < 3; ++k) {
+            qw[k][half] = wl[k];
+            qw[k][2 + half] = wh[k];
+        }
     }
-    nodes[i] = N;
-    for (int k = 0; k < 3; ++k) {
-        box8[6 * (size_t)i + k] = lo[k];
-        box8[6 * (size_t)i + 3 + k] = hi[k];
+    if (s == 0) {
+        const uint32_t ew = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) |
+                            ((uint32_t)(ex[2] + 127) << 16) | (imask << 24);
+        N->a = make_float4(lo[0], lo[1], lo[2], __uint_as_float(ew));
+        for (int k = 0; k < 3; ++k) {
+            box8[6 * (size_t)i + k] = lo[k];
+            box8[6 * (size_t)i + 3 + k] = hi[k];
+        }
     }
 }
 
@@ -336,8 +349,8 @@ int refitBvh8(BvhBuild &b, const float *positions, const int *triIndices, int nu
     for (int l = b.levels8 - 1; l >= 0; --l) {
         const int begin = b.levelOff8[l], end = b.levelOff8[l + 1];
         if (end > begin)
-            kRefitLevel<<<(end - begin + 127) / 128, 128, 0, st>>>(begin, end, b.nodes8, b.triV8, b.box8,
-                                                                  b.numNodes8, numTris);
+            kRefitLevel<<<(8 * (end - begin) + 127) / 128, 128, 0, st>>>(begin, end, b.nodes8, b.triV8, b.box8,
+                                                                        b.numNodes8, numTris);
     }
     return (int)cudaGetLastError();
 }

@@ -352,7 +352,8 @@ void buildHostBvh(const float *P, const int *I, int n, int leafSize, HostBvh &h)
 // it has 8 entries or only leaves; children and triangles are placed by
 // prefix sums in item order; children take their centroid-octant slot (or the
 // nearest free one by Hamming distance); boxes are quantised outwards by one
-// step with a per-axis power-of-two scale computed in double.
+// step with a per-axis power-of-two scale; FP32 with directed rounding
+// (extent up, a child's low offset down and high offset up).
 struct Node8 {
     float p[3];
     uint32_t ew;
@@ -372,14 +373,27 @@ float sa8(const Entry8 &e)
     return (dx * dy + dy * dz) + dz * dx;
 }
 
-int scaleExp(double ext)
+// a - b rounded down / up, from the round-to-nearest difference and its
+// exact error (Knuth's TwoSum), as the device's __fsub_rd / __fsub_ru give.
+float subDown(float a, float b)
 {
-    if (!(ext > 0.0))
+    const float s = a - b, bv = s - a, err = (a - (s - bv)) + (-b - bv);
+    return err < 0.0f ? std::nextafter(s, -INFINITY) : s;
+}
+float subUp(float a, float b)
+{
+    const float s = a - b, bv = s - a, err = (a - (s - bv)) + (-b - bv);
+    return err > 0.0f ? std::nextafter(s, INFINITY) : s;
+}
+
+int scaleExp(float ext)
+{
+    if (!(ext > 0.0f))
         return -126;
     int e = std::ilogb(ext) - 7;
-    while (std::ldexp(253.0, e) < ext)
+    while (std::ldexp(253.0f, e) < ext)
         ++e;
-    while (e > -126 && std::ldexp(253.0, e - 1) >= ext)
+    while (e > -126 && std::ldexp(253.0f, e - 1) >= ext)
         --e;
     return std::max(-126, std::min(127, e));
 }
@@ -486,7 +500,7 @@ void buildHostBvh8(const HostBvh &B, std::vector<Node8> &out, std::vector<int> &
             }
             int ex[3];
             for (int k = 0; k < 3; ++k)
-                ex[k] = scaleExp((double)hi[k] - (double)lo[k]);
+                ex[k] = scaleExp(subUp(hi[k], lo[k]));
             uint32_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0}, ql[3][8] = {}, qh[3][8] = {};
             uint32_t imask = 0;
             const int childBase = nextStart + scanK[i], triBase = triStart + scanT[i];
@@ -496,13 +510,13 @@ void buildHostBvh8(const HostBvh &B, std::vector<Node8> &out, std::vector<int> &
                 if (j < 0)
                     continue;
                 for (int k = 0; k < 3; ++k) {
-                    const double inv = std::ldexp(1.0, -ex[k]);
-                    double a = std::floor(((double)e[j].lo[k] - (double)lo[k]) * inv);
-                    double b = std::ceil(((double)e[j].hi[k] - (double)lo[k]) * inv);
-                    a = a > 0.0 ? a - 1.0 : 0.0;
-                    b = std::fmin(b + 1.0, 255.0);
+                    const float inv = std::ldexp(1.0f, -ex[k]);
+                    float a = std::floor(subDown(e[j].lo[k], lo[k]) * inv);
+                    float b = std::ceil(subUp(e[j].hi[k], lo[k]) * inv);
+                    a = a > 0.0f ? a - 1.0f : 0.0f;
+                    b = std::fmin(b + 1.0f, 255.0f);
                     ql[k][s] = (uint32_t)a;
-                    qh[k][s] = (uint32_t)b;
+                    qh[k][s] = (uint32_t)std::fmax(b, 0.0f);
                 }
                 if (e[j].cnt == 0) {
                     imask |= 1u << s;
