@@ -90,40 +90,21 @@ OPT_D float vmfPdf(const Lobe &L, float3 w)
 {
     return vmfNorm(L.kappa) * expf(L.kappa * (dot3(L.mu, w) - 1.0f));
 }
-OPT_D float mixturePdf(const Mixture &m, float3 w)
+// Direction from a vMF lobe by Jakob's stable inversion ("Numerically
+// stable sampling of the von Mises-Fisher distribution on S^2").
+OPT_D float3 vmfSample(float3 mu, float kappa, float xi1, float xi2)
 {
-    float p = 0.0f;
-#pragma unroll
-    for (int k = 0; k < LOBES; ++k)
-        p += m.lobe[k].weight * vmfPdf(m.lobe[k], w);
-    return p;
-}
-// Lobe by xi0 over the weights; direction by Jakob's stable inversion
-// ("Numerically stable sampling of the von Mises-Fisher distribution on S^2").
-OPT_D float3 mixtureSample(const Mixture &m, float xi0, float xi1, float xi2)
-{
-    int k = LOBES - 1;
-    float acc = 0.0f;
-#pragma unroll
-    for (int j = 0; j < LOBES; ++j) {
-        acc += m.lobe[j].weight;
-        if (xi0 < acc) {
-            k = j;
-            break;
-        }
-    }
-    const Lobe &L = m.lobe[k];
     float w;
-    if (L.kappa < 1e-4f)
+    if (kappa < 1e-4f)
         w = 1.0f - 2.0f * xi1;
     else
-        w = 1.0f + logf(xi1 + (1.0f - xi1) * expf(-2.0f * L.kappa)) / L.kappa;
+        w = 1.0f + logf(xi1 + (1.0f - xi1) * expf(-2.0f * kappa)) / kappa;
     w = fminf(fmaxf(w, -1.0f), 1.0f);
     const float s = sqrtf(fmaxf(0.0f, 1.0f - w * w));
     float sp, cp;
     sincosf(2.0f * OPT_PI * xi2, &sp, &cp);
     // frame around mu (Duff et al. 2017 branchless ONB)
-    const float3 n = L.mu;
+    const float3 n = mu;
     const float sign = copysignf(1.0f, n.z);
     const float a = -1.0f / (sign + n.z), b = n.x * n.y * a;
     const float3 t = mk3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
@@ -180,27 +161,74 @@ OPT_D void pack(const Mixture &m, Packed &p)
     }
     memcpy(&p, h, sizeof(p));
 }
-// Decoded values are what sampling and evaluation both use, so the density
-// the shading kernel evaluates is exactly the one it samples from.
-OPT_D void unpack(const Packed &p, Mixture &m)
+// The shading kernel reads the packed mixture directly (no unpacked copy, so
+// nothing is indexed at run time and it all stays in registers). Sampling
+// and evaluation use the same decoded values, so the density evaluated is
+// exactly the one sampled from: mu renormalised from its halves, kappa,
+// weights normalised to sum 1 (uniform if they are all zero).
+OPT_D float packedHalf(const Packed &p, int i)  // i: a constant after unrolling
 {
-    __half h[48];
-    memcpy(h, &p, sizeof(p));
-    m.select = __half2float(h[40]);
+    const uint4 q = p.q[i >> 3];
+    const int wi = (i >> 1) & 3;
+    const uint32_t w = wi == 0 ? q.x : wi == 1 ? q.y : wi == 2 ? q.z : q.w;
+    return __half2float(__ushort_as_half((unsigned short)((i & 1) ? (w >> 16) : (w & 0xFFFFu))));
+}
+OPT_D float3 packedMu(const Packed &p, int k)
+{
+    const float3 r = mk3(packedHalf(p, 4 * k), packedHalf(p, 4 * k + 1), packedHalf(p, 4 * k + 2));
+    const float len = sqrtf(dot3(r, r));
+    return len > 1e-6f ? r * (1.0f / len) : mk3(0.0f, 0.0f, 1.0f);
+}
+OPT_D float packedSelect(const Packed &p) { return packedHalf(p, 40); }
+OPT_D float packedWeightSum(const Packed &p)
+{
     float sum = 0.0f;
 #pragma unroll
-    for (int k = 0; k < LOBES; ++k) {
-        const float3 mu = mk3(__half2float(h[4 * k]), __half2float(h[4 * k + 1]), __half2float(h[4 * k + 2]));
-        const float len = sqrtf(dot3(mu, mu));
-        m.lobe[k].mu = len > 1e-6f ? mu * (1.0f / len) : mk3(0.0f, 0.0f, 1.0f);
-        m.lobe[k].kappa = __half2float(h[4 * k + 3]);
-        m.lobe[k].weight = __half2float(h[32 + k]);
-        sum += m.lobe[k].weight;
-    }
-    const float inv = sum > 0.0f ? 1.0f / sum : 0.0f;
+    for (int k = 0; k < LOBES; ++k)
+        sum += packedHalf(p, 32 + k);
+    return sum;
+}
+OPT_D float packedWeight(const Packed &p, int k, float sum, float inv)
+{
+    return sum > 0.0f ? packedHalf(p, 32 + k) * inv : 1.0f / LOBES;
+}
+OPT_D float vmfPdfAt(float3 mu, float kappa, float3 w)
+{
+    return vmfNorm(kappa) * expf(kappa * (dot3(mu, w) - 1.0f));
+}
+OPT_D float mixturePdf(const Packed &p, float3 w)
+{
+    const float sum = packedWeightSum(p), inv = sum > 0.0f ? 1.0f / sum : 0.0f;
+    float pdf = 0.0f;
 #pragma unroll
     for (int k = 0; k < LOBES; ++k)
-        m.lobe[k].weight = sum > 0.0f ? m.lobe[k].weight * inv : 1.0f / LOBES;
+        pdf += packedWeight(p, k, sum, inv) * vmfPdfAt(packedMu(p, k), packedHalf(p, 4 * k + 3), w);
+    return pdf;
+}
+// Lobe by xi0 over the weights, then a direction from it.
+OPT_D float3 mixtureSample(const Packed &p, float xi0, float xi1, float xi2)
+{
+    const float sum = packedWeightSum(p), inv = sum > 0.0f ? 1.0f / sum : 0.0f;
+    float acc = 0.0f;
+    int k = LOBES - 1;
+    bool found = false;
+#pragma unroll
+    for (int j = 0; j < LOBES; ++j) {
+        acc += packedWeight(p, j, sum, inv);
+        if (!found && xi0 < acc) {
+            k = j;
+            found = true;
+        }
+    }
+    float3 mu = packedMu(p, LOBES - 1);
+    float kappa = packedHalf(p, 4 * (LOBES - 1) + 3);
+#pragma unroll
+    for (int j = 0; j < LOBES - 1; ++j)
+        if (j == k) {
+            mu = packedMu(p, j);
+            kappa = packedHalf(p, 4 * j + 3);
+        }
+    return vmfSample(mu, kappa, xi1, xi2);
 }
 
 }  // namespace guide

@@ -610,16 +610,15 @@ __global__ void __launch_bounds__(256) kShade(DevScene s, FrameParams fp, WaveBu
                                 // One-sample MIS of the learned mixture and the lobe's own
                                 // sampler. The lobe's density decides the kill test, as in
                                 // the plain estimator, so both integrate over the same set.
-                                guide::Mixture gm;
                                 // primary hits of one pixel share its first sample's mixture
                                 const uint32_t mi =
                                     depth == 1 && gp.sharePrimary
                                         ? i % (fp.batch.on ? __ldg(fp.batch.dyn) : fp.npix)
                                         : i;
-                                guide::unpack(reinterpret_cast<const guide::Packed *>(gp.mix)[mi], gm);
+                                const guide::Packed gm = reinterpret_cast<const guide::Packed *>(gp.mix)[mi];
                                 // selection probability: the network's, phased in with training
-                                const float alpha =
-                                    ramp * fminf(fp.guide.alphaMax, fmaxf(fp.guide.alphaMin, gm.select));
+                                const float alpha = ramp * fminf(fp.guide.alphaMax,
+                                                                 fmaxf(fp.guide.alphaMin, guide::packedSelect(gm)));
                                 const float uSel = U.next();
                                 if (uSel < alpha)
                                     smp.dir = guide::mixtureSample(gm, xi.x, 1.0f - xi.y, xi.z);
