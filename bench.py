@@ -175,13 +175,17 @@ def guided_equal_time(stream, budget_s=None, reference_spp=None):
     ref = make(1000, 0)
     ref.render(g["reference_spp"], stream)
     torch.cuda.synchronize()
-    s, _, n = ref.accum()
+    s, q, n = ref.accum()
     R = s.reshape(-1, 3) / n
+    # variance of the reference's per-pixel mean (FP64 sum of squares): the
+    # reference's own noise, which adds to every render's measured error
+    var_ref = np.maximum(q.reshape(-1, 3) / n - R * R, 0.0) / (n - 1)
+    den = R ** 2 + 1e-2
     ref_seconds = time.perf_counter() - t0
     ref.close()
     out = {}
     for mode, name in ((0, "plain"), (1, "guided")):
-        errs, spps, mrays = [], [], []
+        errs, errs_c, spps, mrays = [], [], [], []
         for seed in g["seeds"]:
             r = make(seed, mode)
             batch = r.stats()["sppBatch"]
@@ -197,13 +201,23 @@ def guided_equal_time(stream, budget_s=None, reference_spp=None):
             st1 = r.stats()
             s, _, n = r.accum()
             I = s.reshape(-1, 3) / n
-            errs.append(float(np.mean(((I - R) ** 2 / (R ** 2 + 1e-2)).sum(1))))
+            errs.append(float(np.mean(((I - R) ** 2 / den).sum(1))))
+            errs_c.append(float(np.mean((((I - R) ** 2 - var_ref) / den).sum(1))))
             spps.append(spp)
             mrays.append((st1["extensionRays"] - st0["extensionRays"] + st1["shadowRays"] - st0["shadowRays"]) / dt / 1e6)
             r.close()
         out[name] = {"relmse": float(np.mean(errs)), "relmse_per_seed": errs, "spp_in_budget": spps,
-                     "mrays_per_s": float(np.mean(mrays))}
+                     "mrays_per_s": float(np.mean(mrays)),
+                     "relmse_reference_noise_removed": float(np.mean(errs_c))}
     out["relmse_ratio_plain_over_guided"] = out["plain"]["relmse"] / out["guided"]["relmse"]
+    # The same ratio with the reference's own variance (estimated per pixel
+    # from its sum of squares) subtracted from each render's squared error.
+    # The renders and the reference draw independent samples, so this
+    # estimates each render's error against the noise-free image (the
+    # denominators still use the reference). Reported beside the protocol's
+    # ratio, which stays the headline.
+    out["relmse_ratio_reference_noise_removed"] = (out["plain"]["relmse_reference_noise_removed"] /
+                                                   out["guided"]["relmse_reference_noise_removed"])
     out["config"] = dict(g, reference_seconds=ref_seconds,
                          protocol="equal wall time per seed, online training inside the guided budget; "
                                   "relMSE is the mean over seeds of each render's relMSE")
