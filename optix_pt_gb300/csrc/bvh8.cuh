@@ -41,6 +41,35 @@ OPT_D float byteToFloat(uint32_t w, int k)
     return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)k)) - 8388608.0f;
 }
 
+// Three-input minimum and maximum (PTX `min.f32` / `max.f32` with three
+// sources, sm_100 and later). NaN operands are ignored, as by fminf / fmaxf,
+// so the result equals the two-input chain bit for bit.
+OPT_D float min3f(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+OPT_D float max3f(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Bit s of m moved to bit s ^ oct (8-bit masks): adjacent bits, pairs and
+// nibbles swap for oct bits 0, 1 and 2.
+OPT_D uint32_t octantOrder(uint32_t m, uint32_t oct)
+{
+    if (oct & 1u)
+        m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u)
+        m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u)
+        m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+    return m;
+}
+
 // Traversal state of one ray: registers, plus the node-group stack in local
 // memory. `step` visits one node (and the triangles of the leaf children the
 // ray reaches) and reports whether the ray is finished.
@@ -95,8 +124,7 @@ struct Trav8 {
         const uint32_t nx0 = px ? qx.x : qx.z, nx1 = px ? qx.y : qx.w, fx0 = px ? qx.z : qx.x, fx1 = px ? qx.w : qx.y;
         const uint32_t ny0 = py ? qy.x : qy.z, ny1 = py ? qy.y : qy.w, fy0 = py ? qy.z : qy.x, fy1 = py ? qy.w : qy.y;
         const uint32_t nz0 = pz ? qz.x : qz.z, nz1 = pz ? qz.y : qz.w, fz0 = pz ? qz.z : qz.x, fz1 = pz ? qz.w : qz.y;
-        const float tlim = tcur * BOX_WIDEN;
-        uint32_t ihits = 0, lhits = 0;
+        uint32_t hm = 0;
 #pragma unroll
         // Empty slots are not skipped: their boxes are the single point at the
         // node's origin (all-zero quantised bounds), which a ray reaches only
@@ -110,15 +138,14 @@ struct Trav8 {
             const float yf = fmaf(byteToFloat(s < 4 ? fy0 : fy1, k), ays, by);
             const float zn = fmaf(byteToFloat(s < 4 ? nz0 : nz1, k), azs, bz);
             const float zf = fmaf(byteToFloat(s < 4 ? fz0 : fz1, k), azs, bz);
-            const float tn = fmaxf(fmaxf(xn, yn), fmaxf(zn, tmin));
-            const float tf = fminf(fminf(xf, yf), zf) * BOX_WIDEN;
-            if (tn <= fminf(tf, tlim)) {
-                if ((imask >> s) & 1u)
-                    ihits |= 1u << ((uint32_t)s ^ oct);
-                else
-                    lhits |= 1u << s;
-            }
+            // far plane: min(tf * w, tcur * w) == min(tf, tcur) * w exactly
+            // (scaling by w > 0 and rounding are both monotone)
+            const float tn = max3f(xn, yn, fmaxf(zn, tmin));
+            const float tf = min3f(xf, yf, fminf(zf, tcur)) * BOX_WIDEN;
+            hm |= (tn <= tf ? 1u : 0u) << s;
         }
+        uint32_t lhits = hm & ~imask;
+        const uint32_t ihits = octantOrder(hm & imask, oct);
         // Leaf children: their triangles, now.
         while (lhits) {
             const int s = __ffs(lhits) - 1;
