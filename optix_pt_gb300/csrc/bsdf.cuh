@@ -286,71 +286,116 @@ OPT_D float3 sheenBrdf(const MatMR &m, float3 l, float3 v)
 
 // metallicRoughnessBrdf (principled_bsdf.h:866-898) with dielectricBrdf
 // (:638-681), which draws one uniform for transmissive materials (:649).
+// The reference's branches pick a lobe first; each lobe is then evaluated at
+// one place in the code (the shading kernel's speed is bound by instruction
+// fetch, and every inlined copy of a lobe adds to what it fetches).
 template <class U> OPT_D float3 evalBrdf(const MatMR &m, float3 l, float3 v, U &u)
 {
     const uint32_t c = m.category;
-    if (c & MF_METAL)
-        return metalBrdf(m, l, v);
-    if (c & MF_DIELECTRIC) {
+    int lobe = 4;  // 0 GGX / mirror reflection, 1 transmission, 2 diffuse, 3 sheen, 4 none
+    if (c & MF_METAL) {
+        lobe = 0;
+    } else if (c & MF_DIELECTRIC) {
         if (c & MF_TRANSMISSION) {
             float F = schlick(calcF0(m.ior), dot3(v, m.n));
             float xi = u.next();
-            return xi < F ? reflectionBrdf(m, l, v) : transmissionBrdf(m, l, v);
+            lobe = xi < F ? 0 : 1;
+        } else {
+            lobe = (c & MF_REFLECTION) ? 0 : 2;
         }
-        if (c & MF_REFLECTION)
-            return reflectionBrdf(m, l, v);
-        return diffuseBrdf(m, l, v);
+    } else if (c & MF_COAT) {
+        lobe = 0;
+    } else if (c & MF_SHEEN) {
+        lobe = 3;
     }
-    if (c & MF_COAT)
-        return reflectionBrdf(m, l, v);
-    if (c & MF_SHEEN)
+    if (lobe == 0) {
+        const float3 fs = reflectionBrdf(m, l, v);
+        if (!(c & MF_METAL))
+            return fs;
+        // metalBrdf (principled_bsdf.h:748-762): conductor Fresnel on top
+        const float3 h = normalize3(l + v);
+        const float p = schlickPow(dot3(v, h));
+        return fs * (m.baseColour + (mk3s(1.0f) - m.baseColour) * p);
+    }
+    if (lobe == 1)
+        return transmissionBrdf(m, l, v);
+    if (lobe == 2)
+        return diffuseBrdf(m, l, v);
+    if (lobe == 3)
         return sheenBrdf(m, l, v);
     return mk3(1.0f, 0.0f, 1.0f);
 }
 
 // metallicRoughnessSample (principled_bsdf.h:902-961) with metalSample
-// (:769-785), dielectricSample (:683-735), sheenSample (:852-859).
+// (:769-785), dielectricSample (:683-735), sheenSample (:852-859); lobe first,
+// as in evalBrdf. Metal and sheen take reflectionDir's direction without
+// reflectionSample's validity test, as the reference does.
 template <class U> OPT_D bool sampleBrdf(const MatMR &m, float3 wo, float3 xi, U &u, Sample &s)
 {
     const uint32_t c = m.category;
+    // 0 metal, 1 GGX / mirror reflection, 2 transmission, 3 diffuse, 4 sheen, 5 none
+    int lobe = 5;
+    bool fresnelSplit = false;  // transmissive dielectric: reflection F, transmission 1 - F
+    float F = 0.0f;
     if (c & MF_METAL) {
-        s.dir = reflectionDir(m, wo, xi.x, xi.y);
-        s.pdf = reflectionPdf(m, s.dir, wo);
-        s.bsdf = metalBrdf(m, s.dir, wo);
-        return true;
-    }
-    if (c & MF_DIELECTRIC) {
+        lobe = 0;
+    } else if (c & MF_DIELECTRIC) {
         if (c & MF_TRANSMISSION) {
-            float F = schlick(fminf(calcF0(m.ior), 1.0f), dot3(wo, m.n));
+            F = schlick(fminf(calcF0(m.ior), 1.0f), dot3(wo, m.n));
             float r1 = u.next();
-            bool ret;
-            if (r1 < F) {
-                ret = reflectionSample(m, wo, xi.x, xi.y, s);
-                s.bsdf = s.bsdf * F;
-                s.pdf = s.pdf * F;
-            } else {
-                ret = transmissionSample(m, wo, xi.x, xi.y, s);
-                s.bsdf = s.bsdf * (1.0f - F);
-                s.pdf = s.pdf * (1.0f - F);
-            }
-            return ret;
+            fresnelSplit = true;
+            lobe = r1 < F ? 1 : 2;
+        } else {
+            lobe = (c & MF_REFLECTION) ? 1 : 3;
         }
-        if (c & MF_REFLECTION)
-            return reflectionSample(m, wo, xi.x, xi.y, s);
-        return diffuseSample(m, wo, xi.x, xi.y, s);
+    } else if (c & MF_COAT) {
+        lobe = 1;
+    } else if (c & MF_SHEEN) {
+        lobe = 4;
     }
-    if (c & MF_COAT)
-        return reflectionSample(m, wo, xi.x, xi.y, s);
-    if (c & MF_SHEEN) {
+    bool ret = true;
+    if (lobe == 1 && (c & MF_SPECULAR)) {
+        ret = specReflSample(m, wo, s);
+    } else if (lobe == 0 || lobe == 1 || lobe == 4) {
         s.dir = reflectionDir(m, wo, xi.x, xi.y);
-        s.bsdf = sheenBrdf(m, s.dir, wo);
+        if (lobe == 4) {
+            s.bsdf = sheenBrdf(m, s.dir, wo);
+            s.pdf = 1.0f;
+        } else {
+            // reflectionSample (principled_bsdf.h:483-520) rejects directions
+            // below the surface or against the half vector; metal does not
+            const float3 h = normalize3(s.dir + wo);
+            if (lobe == 0 || (dot3(s.dir, h) > 0.0f && dot3(s.dir, m.n) > 0.0f)) {
+                s.pdf = reflectionPdf(m, s.dir, wo);
+                const float3 fs = reflectionBrdf(m, s.dir, wo);
+                if (lobe == 0) {
+                    // metalBrdf: conductor Fresnel on top
+                    const float p = schlickPow(dot3(wo, h));
+                    s.bsdf = fs * (m.baseColour + (mk3s(1.0f) - m.baseColour) * p);
+                } else {
+                    s.bsdf = fs;
+                }
+            } else {
+                s.bsdf = mk3s(0.0f);
+                s.pdf = 0.0f;
+                ret = false;
+            }
+        }
+    } else if (lobe == 2) {
+        ret = transmissionSample(m, wo, xi.x, xi.y, s);
+    } else if (lobe == 3) {
+        ret = diffuseSample(m, wo, xi.x, xi.y, s);
+    } else {
+        s.dir = mk3(0.0f, 1.0f, 0.0f);
+        s.bsdf = mk3(1.0f, 0.0f, 1.0f);
         s.pdf = 1.0f;
-        return true;
     }
-    s.dir = mk3(0.0f, 1.0f, 0.0f);
-    s.bsdf = mk3(1.0f, 0.0f, 1.0f);
-    s.pdf = 1.0f;
-    return true;
+    if (fresnelSplit) {
+        const float k = lobe == 1 ? F : 1.0f - F;
+        s.bsdf = s.bsdf * k;
+        s.pdf = s.pdf * k;
+    }
+    return ret;
 }
 
 // Lobes a learned proposal may be mixed with (one-sample MIS): those whose
