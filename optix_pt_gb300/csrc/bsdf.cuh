@@ -165,8 +165,8 @@ OPT_D float3 diffuseBrdf(const MatMR &m, float3 l, float3 v)
         return m.baseColour * OPT_INV_PI;
     return orenNayar(m, l, v);
 }
-// diffuseSample (principled_bsdf.h:245-279) with cosineSampleHemisphere (sampling.h:27-42)
-OPT_D bool diffuseSample(const MatMR &m, float3 v, float x, float y, Sample &s)
+// cosineSampleHemisphere (sampling.h:27-42) around n
+OPT_D float3 cosineDir(float3 n, float x, float y)
 {
     float r = sqrtf(x);
     float phi = y * 2.0f * OPT_PI;
@@ -174,7 +174,12 @@ OPT_D bool diffuseSample(const MatMR &m, float3 v, float x, float y, Sample &s)
     sincosf(phi, &sp, &cp);
     float px = r * cp, py = r * sp;
     float z = sqrtf(fmaxf(0.0f, 1.0f - px * px - py * py));
-    s.dir = onbToWorld(m.n, mk3(px, py, z));
+    return onbToWorld(n, mk3(px, py, z));
+}
+// diffuseSample (principled_bsdf.h:245-279)
+OPT_D bool diffuseSample(const MatMR &m, float3 v, float x, float y, Sample &s)
+{
+    s.dir = cosineDir(m.n, x, y);
     s.bsdf = diffuseBrdf(m, s.dir, v);
     s.pdf = dot3(m.n, s.dir) * OPT_INV_PI;
     return true;
@@ -427,6 +432,16 @@ OPT_D float lobePdf(const MatMR &m, float3 l, float3 v)
         return (dot3(l, h) > 0.0f && dot3(l, m.n) > 0.0f) ? reflectionPdf(m, l, v) : 0.0f;
     }
     return dot3(m.n, l) * OPT_INV_PI;  // cosine-weighted diffuse
+}
+// Direction sampleBrdf draws for a guidable lobe, by the same arithmetic
+// (these lobes draw no extra uniforms); its value and density at that
+// direction are lobeValue's and lobePdf's.
+OPT_D float3 lobeDir(const MatMR &m, float3 wo, float3 xi)
+{
+    const uint32_t c = m.category;
+    if ((c & MF_METAL) || reflectionLobe(c))
+        return reflectionDir(m, wo, xi.x, xi.y);
+    return cosineDir(m.n, xi.x, xi.y);
 }
 // Value sampleBrdf reports for direction l of a guidable lobe.
 OPT_D float3 lobeValue(const MatMR &m, float3 l, float3 v)

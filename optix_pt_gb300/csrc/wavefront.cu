@@ -624,10 +624,10 @@ __global__ void __maxnreg__(64) kShade(DevScene s, FrameParams fp, WaveBufs q, i
                                 const float alpha = ramp * fminf(fp.guide.alphaMax,
                                                                  fmaxf(fp.guide.alphaMin, guide::packedSelect(gm)));
                                 const float uSel = U.next();
-                                if (uSel < alpha)
-                                    smp.dir = guide::mixtureSample(gm, xi.x, 1.0f - xi.y, xi.z);
-                                else
-                                    bsdf::sampleBrdf(m, wo, xi, U, smp);
+                                // the lobe's own sampler: its direction only (value and
+                                // density follow for either strategy's direction)
+                                smp.dir = uSel < alpha ? guide::mixtureSample(gm, xi.x, 1.0f - xi.y, xi.z)
+                                                       : bsdf::lobeDir(m, wo, xi);
                                 const float pc = bsdf::lobePdf(m, smp.dir, wo);
                                 pcLobe = pc;
                                 smp.bsdf = bsdf::lobeValue(m, smp.dir, wo);
