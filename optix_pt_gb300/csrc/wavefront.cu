@@ -362,7 +362,6 @@ __global__ void __maxnreg__(64) kShade(DevScene s, FrameParams fp, WaveBufs q, i
     __shared__ BlockPushScratch pushScratch;
     // warp-granular compaction walks the queue by warps; block-granular by
     // blocks, so that every thread of a block makes the same number of trips
-    const uint32_t chunk = BLOCKPUSH ? blockDim.x : 32u;
     const uint32_t first = BLOCKPUSH ? blockIdx.x * blockDim.x : warpId * 32u;
     const uint32_t step = BLOCKPUSH ? gridDim.x * blockDim.x : nWarps * 32u;
     for (uint32_t base = first; base < count; base += step) {
