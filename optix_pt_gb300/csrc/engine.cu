@@ -95,6 +95,11 @@ struct optpt_renderer {
     cudaGraphExec_t graphExec = nullptr;
     bool graphDirty = true;
     cudaStream_t ownStream = nullptr;
+    // Side stream of a pass: each bounce's shadow launches run on it, beside
+    // the next bounce's extension (fork after shading, join before the next
+    // shading).
+    cudaStream_t sideStream = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
 
     FrameConst *dFrameConst = nullptr;
 
@@ -281,6 +286,12 @@ struct optpt_renderer {
         cudaFree(dVShape);
         cudaFree(dJoints);
         cudaFree(dWeights);
+        if (evFork)
+            cudaEventDestroy(evFork);
+        if (evJoin)
+            cudaEventDestroy(evJoin);
+        if (sideStream)
+            cudaStreamDestroy(sideStream);
         if (ownStream)
             cudaStreamDestroy(ownStream);
     }
@@ -390,6 +401,14 @@ int enqueuePassOn(optpt_renderer *r, const FrameParams &fp, const WaveBufs &q, c
     cudaMemsetAsync(q.counters, 0, sizeof(uint32_t) * CNT_TOTAL, st);
     if (fp.guide.train)
         cudaMemsetAsync(fp.guide.batchCount, 0, sizeof(uint32_t), st);
+    // Bounce d's shadow rays and bounce d + 1's extension rays are
+    // independent (the shadow launches add to the path radiance, which only
+    // the next shading reads), so the shadow launches go to the side stream
+    // and overlap the next extension (and inference). Past the first bounces
+    // the queues are short and every launch is bound by its longest ray, so
+    // running them side by side hides one behind the other. Timed profiling
+    // and the counting variant keep one stream.
+    const bool fork = ev == nullptr && !count && r->sideStream != nullptr;
     mark(0);
     launchGenerate(r->shape, fp, q, st);
     for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
@@ -399,12 +418,24 @@ int enqueuePassOn(optpt_renderer *r, const FrameParams &fp, const WaveBufs &q, c
             mark(5);
             launchGuideInfer(r->guide, r->scene, fp, q, (int)d, st);
         }
+        if (fork && d > 1)
+            cudaStreamWaitEvent(st, r->evJoin, 0);  // bounce d - 1's shadow rays resolved
         mark(2);
         launchShade(r->shape, r->scene, fp, q, (int)d, st);
         mark(3);
-        launchShadow(r->shape, r->scene, fp, q, (int)d, 0, st, count);
-        launchShadow(r->shape, r->scene, fp, q, (int)d, 1, st, count);
+        if (fork) {
+            cudaEventRecord(r->evFork, st);
+            cudaStreamWaitEvent(r->sideStream, r->evFork, 0);
+            launchShadow(r->shape, r->scene, fp, q, (int)d, 0, r->sideStream, count);
+            launchShadow(r->shape, r->scene, fp, q, (int)d, 1, r->sideStream, count);
+            cudaEventRecord(r->evJoin, r->sideStream);
+        } else {
+            launchShadow(r->shape, r->scene, fp, q, (int)d, 0, st, count);
+            launchShadow(r->shape, r->scene, fp, q, (int)d, 1, st, count);
+        }
     }
+    if (fork)
+        cudaStreamWaitEvent(st, r->evJoin, 0);  // the last bounce's shadow rays
     if (fp.guide.train) {
         // online training on this pass's samples (before the pass count advances)
         mark(6);
@@ -687,7 +718,10 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
     int rc = OPTPT_OK;
     cudaError_t e;
     do {
-        if ((e = cudaStreamCreateWithFlags(&r->ownStream, cudaStreamNonBlocking)) != cudaSuccess) {
+        if ((e = cudaStreamCreateWithFlags(&r->ownStream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaStreamCreateWithFlags(&r->sideStream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&r->evFork, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&r->evJoin, cudaEventDisableTiming)) != cudaSuccess) {
             rc = cudaFail(e, "stream");
             break;
         }
