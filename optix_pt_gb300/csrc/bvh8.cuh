@@ -227,6 +227,12 @@ OPT_D void traverse8Queue(const Bvh8Node *__restrict__ nodes, const float4 *__re
                           uint32_t *next, Fetch fetch, Finish finish, AlphaFn alpha, Counter &ctr)
 {
     const uint32_t lane = threadIdx.x & 31u;
+    // The first 32 rays of every warp come in queue order without the
+    // counter (warp w takes w * 32 .. w * 32 + 31): no burst of atomics on
+    // one address when the grid starts, and none at all when the queue is
+    // shorter than the grid. The counter hands out the rest, from there on.
+    const uint32_t firstRound = (gridDim.x * blockDim.x) & ~31u;
+    bool started = false;
     Trav8 T;
     HitRec hit;
     hit.leaf = -1;
@@ -237,12 +243,18 @@ OPT_D void traverse8Queue(const Bvh8Node *__restrict__ nodes, const float4 *__re
         const unsigned nm = __ballot_sync(0xffffffffu, need);
         // Refill in batches: a fetch stalls the whole warp on the atomic, so
         // wait until enough lanes are idle (or none is busy).
-        if (nm && (__popc(nm) >= TRAV8_REFILL || __ballot_sync(0xffffffffu, ray >= 0) == 0u)) {
+        if (nm && (!started || __popc(nm) >= TRAV8_REFILL || __ballot_sync(0xffffffffu, ray >= 0) == 0u)) {
             const int leader = __ffs(nm) - 1;
-            uint32_t base = 0;
-            if ((int)lane == leader)
-                base = atomicAdd(next, (uint32_t)__popc(nm));
-            base = __shfl_sync(0xffffffffu, base, leader);
+            uint32_t base;
+            if (!started) {
+                base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;  // this warp's first 32
+                started = true;
+            } else {
+                base = 0;
+                if ((int)lane == leader)
+                    base = atomicAdd(next, (uint32_t)__popc(nm));
+                base = __shfl_sync(0xffffffffu, base, leader) + firstRound;
+            }
             if (need) {
                 const uint32_t i = base + (uint32_t)__popc(nm & ((1u << lane) - 1u));
                 if (i < count) {
