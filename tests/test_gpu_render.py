@@ -69,6 +69,31 @@ def test_graph_and_direct_launch_are_identical(cuda_dev):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("scene", ["cornell", "spheres"])
+def test_overlapped_shadow_branch_matches_one_stream(cuda_dev, scene):
+    """A pass runs each bounce's shadow launches on a side stream beside the
+    next bounce's extension; the timed-profile pass runs the same launches on
+    one stream. Both must accumulate the same bits."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural(scene)
+    outs = []
+    for profiled in (False, True):
+        r = opt.Renderer(sc, spp_batch=2)
+        r.setupOutputBuffer(96, 64)
+        if profiled:
+            for _ in range(3):
+                r.profile(2, torch.cuda.current_stream())
+        else:
+            r.render(6, torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        outs.append(r.accum())
+        assert r.getSampleCount() == 6
+        r.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
 def test_camera_change_needs_no_recapture(cuda_dev):
     """Camera and tone settings live in device memory: moving the camera
     between renders changes the image without rebuilding the graph."""
