@@ -336,12 +336,14 @@ OPT_D float4 texAt(const DevScene &s, int tex, float4 tf, float2 tc)
 // (cu/path_tracer.cu:17-582), miss (cu/device_programs.cu:168-174).
 // GUIDED: the learned-guiding variant (mixture sampling and training
 // records); the plain variant carries none of that code.
-// 64 registers (eight 128-thread blocks per SM) with some spilling to L1
+// 72 registers (seven 128-thread blocks per SM) with some spilling to L1
 // beats the 124 the compiler would take: the kernel waits on scattered
 // material, vertex and texture reads, and more resident warps hide them
-// (measured: 1.43 -> 1.27 ms per 1080p sweep pass; 96 and 80 in between).
+// (measured on the 1080p sweep: 1.43 -> 1.27 ms per pass at 64 registers,
+// 96 and 80 in between; with one copy of each BSDF lobe, 72 is 0.9 % ahead
+// of 64 on the sweep and 56 behind).
 template <bool GUIDED, bool BLOCKPUSH>
-__global__ void __maxnreg__(64) kShade(DevScene s, FrameParams fp, WaveBufs q, int depth)
+__global__ void __maxnreg__(72) kShade(DevScene s, FrameParams fp, WaveBufs q, int depth)
 {
     const uint32_t count = q.counters[CNT_EXT + depth];
     const int lane = threadIdx.x & 31;
