@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -68,8 +69,8 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/optpt_clocks.csv"
+        # the raw samples go to $OPTPT_CLOCKS_CSV if set, else to a temporary file
+        self.path = os.environ.get("OPTPT_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(), "optpt_clocks.csv")
 
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
