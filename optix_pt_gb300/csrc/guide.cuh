@@ -220,14 +220,21 @@ OPT_D float3 mixtureSample(const Packed &p, float xi0, float xi1, float xi2)
             found = true;
         }
     }
-    float3 mu = packedMu(p, LOBES - 1);
-    float kappa = packedHalf(p, 4 * (LOBES - 1) + 3);
+    // the chosen lobe's halves first, then one normalisation (packedMu's
+    // arithmetic on them)
+    float rx = packedHalf(p, 4 * (LOBES - 1)), ry = packedHalf(p, 4 * (LOBES - 1) + 1),
+          rz = packedHalf(p, 4 * (LOBES - 1) + 2), kappa = packedHalf(p, 4 * (LOBES - 1) + 3);
 #pragma unroll
     for (int j = 0; j < LOBES - 1; ++j)
         if (j == k) {
-            mu = packedMu(p, j);
+            rx = packedHalf(p, 4 * j);
+            ry = packedHalf(p, 4 * j + 1);
+            rz = packedHalf(p, 4 * j + 2);
             kappa = packedHalf(p, 4 * j + 3);
         }
+    const float3 r = mk3(rx, ry, rz);
+    const float len = sqrtf(dot3(r, r));
+    const float3 mu = len > 1e-6f ? r * (1.0f / len) : mk3(0.0f, 0.0f, 1.0f);
     return vmfSample(mu, kappa, xi1, xi2);
 }
 
