@@ -199,7 +199,16 @@ typedef struct optpt_options {
     uint32_t bvhWidth;   /* 8: compressed 8-wide BVH (default), 2: the binary LBVH   */
     uint32_t compaction; /* queue appends: 0 = auto (one atomic per warp), 32 = per
                           * warp, 1 = per block (one atomic per block and queue)   */
+    uint32_t nodeBudget; /* BVH nodes one ray may visit before its walk is cut short
+                          * (0 = 2^26, more than any walk of a valid tree needs); a
+                          * cut-short walk is counted in optpt_stats               */
+    uint32_t tailBounce; /* plain sampling: from this bounce on, one launch finishes
+                          * every remaining path (closest hit, shading and shadow
+                          * rays per bounce, bit-identical to the per-bounce
+                          * kernels) instead of a launch per kernel per bounce;
+                          * 0 = OPTPT_DEFAULT_TAIL_BOUNCE, 0xFFFFFFFF = never      */
 } optpt_options;
+#define OPTPT_DEFAULT_TAIL_BOUNCE 3
 
 /* Uploads the scene and builds the BVH on the GPU. Replaces the reference's
  * init sequence Renderer(SceneDesc&) .. loadScene() .. buildAccel(true)
@@ -346,6 +355,17 @@ typedef struct optpt_stats {
     uint32_t bvhWidth;       /* BVH traversed: 8 or 2                                */
     uint32_t sppBatch;
     uint32_t blockSize;
+    /* Traversal faults, which leave a ray's result possibly wrong and are
+     * therefore counted rather than silent (zero on every valid BVH; the
+     * reference's OptiX traversal reports none): node groups dropped because
+     * a ray's traversal stack was full (binary BVH; the 8-wide BVH's stack
+     * cannot overflow, since optpt_create refuses trees deeper than its 64
+     * entries), and walks cut short by the node budget
+     * (optpt_options.nodeBudget). Rendered and traced rays both count. */
+    uint64_t traversalStackOverflows;
+    uint64_t traversalBudgetExhausted;
+    uint32_t bvh8Levels;     /* levels of the 8-wide BVH (<= 64)                    */
+    uint32_t pad;
 } optpt_stats;
 int optpt_get_stats(optpt_renderer *r, optpt_stats *out);
 
@@ -353,10 +373,11 @@ int optpt_get_stats(optpt_renderer *r, optpt_stats *out);
  * without a graph with CUDA events around each kernel on `stream`. Index:
  * 0 generate, 1 extend (closest hit), 2 shade, 3 shadow (occlusion),
  * 4 accumulate + tone map, 5 guiding inference, 6 guiding training (sample
- * gather, gradients, Adam). Also returns the rays each kernel class traced. */
+ * gather, gradients, Adam), 7 path completion (the bounces from tailBounce
+ * on). Also returns the rays each kernel class traced. */
 typedef struct optpt_kernel_times {
-    double ms[7];
-    uint64_t launches[7];
+    double ms[8];
+    uint64_t launches[8];
     uint64_t extensionRays;
     uint64_t shadowRays;
 } optpt_kernel_times;
@@ -397,16 +418,20 @@ int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32
                  void *stream);
 
 /* optpt_relmse for callers that cannot allocate device memory when they call
- * it: code running inside a CUDA stream capture, frame loops that forbid
- * allocator calls, or hosts whose own pool owns the device memory. No
- * counterpart in the reference. Same arguments and result; it calls no
- * cudaMalloc, cudaFree or other allocating routine. The partial sums use a
- * fixed 32 KiB array in the library's device memory, which every GPU that
- * loads the library holds until exit; it limits images to 8,388,608 pixels
- * (OPTPT_ERR_INVALID beyond that). The first call on a device looks up that
- * array's address (with the device current), so make the first call before
- * any stream capture. All calls share the array: calls that overlap on the
- * GPU (different streams, no ordering) race and must be avoided. */
+ * it: a progressive viewer's frame loop that must make no allocator call per
+ * frame (cudaMalloc / cudaFree can synchronise the device and stall the
+ * frame), or a host application whose own memory pool owns all device memory
+ * and forbids a library to allocate behind it. No counterpart in the
+ * reference. Same arguments and result; it calls no cudaMalloc, cudaFree or
+ * other allocating routine. The partial sums use a fixed 32 KiB array in the
+ * library's device memory, which every GPU that loads the library holds until
+ * exit; it limits images to 8,388,608 pixels (OPTPT_ERR_INVALID beyond that,
+ * before any device work). The first call on a device looks up that array's
+ * address (with the device current) and caches it, so make the first call
+ * before any stream capture, and do not call it on a device after a
+ * cudaDeviceReset (the cached address is then stale). All calls share the
+ * array, and each call rewrites every entry it reads: calls that overlap on
+ * the GPU (different streams, no ordering) race and must be avoided. */
 int optpt_relmse_noalloc(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
                          void *stream);
 

@@ -113,6 +113,21 @@ class Scene:
         return out
 
 
+    def save(self, path):
+        """Writes the scene arrays, material and light records and textures to
+        an .npz file that the oracle can read without this library
+        (oracle.scene_file.load)."""
+        a = self.arrays()
+        out = {k: v for k, v in a.items() if v is not None and k not in ("materials", "lights")}
+        out["materials"] = np.frombuffer(a["materials"], np.uint8)
+        out["lights"] = np.frombuffer(a["lights"], np.uint8)
+        for i, t in enumerate(self.textures()):
+            out["texture%d" % i] = t["rgba"]
+            out["texture%d_modes" % i] = np.array([t["wrapS"], t["wrapT"], t["srgb"], t["filter"]], np.int32)
+        out["numTextures"] = len(self.textures())
+        np.savez(path, **out)
+
+
 def _decode(fn, data):
     img = _ffi.Image()
     buf = ctypes.create_string_buffer(bytes(data), len(data))
@@ -237,9 +252,13 @@ SceneDesc = Scene.from_config  # the reference constructs SceneDesc from the sce
 class Renderer:
     """The reference's Renderer (include/renderer.h:19-206) on the GB300 engine."""
 
-    def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True, bvh_width=8, compaction=0):
+    def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True, bvh_width=8, compaction=0,
+                 node_budget=0, tail_bounce=0):
+        """tail_bounce: first bounce finished by the path-completion kernel
+        (0 = the library's default, -1 = none: per-bounce kernels only)."""
         self.scene = scene
-        opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0, bvh_width, compaction)
+        opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0, bvh_width, compaction,
+                           node_budget, tail_bounce & 0xFFFFFFFF)
         h = ctypes.c_void_p()
         check(lib.optpt_create(ctypes.byref(scene.struct), ctypes.byref(opt), ctypes.byref(h)))
         self._h = h
@@ -453,7 +472,7 @@ class Renderer:
     def profile(self, spp, stream=None):
         kt = _ffi.KernelTimes()
         check(lib.optpt_render_profiled(self._h, spp, _stream_handle(stream), ctypes.byref(kt)))
-        names = ["generate", "extend", "shade", "shadow", "accumulate", "guide_infer", "guide_train"]
+        names = ["generate", "extend", "shade", "shadow", "accumulate", "guide_infer", "guide_train", "finish"]
         return {"ms": dict(zip(names, list(kt.ms))), "launches": dict(zip(names, list(kt.launches))),
                 "extensionRays": kt.extensionRays, "shadowRays": kt.shadowRays}
 

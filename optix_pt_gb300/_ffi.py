@@ -111,18 +111,21 @@ class SceneStruct(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32), ("leafSize", ctypes.c_uint32),
-                ("useGraph", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32), ("compaction", ctypes.c_uint32)]
+                ("useGraph", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32), ("compaction", ctypes.c_uint32),
+                ("nodeBudget", ctypes.c_uint32), ("tailBounce", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("extensionRays", ctypes.c_uint64), ("shadowRays", ctypes.c_uint64),
                 ("pathSamples", ctypes.c_uint64), ("nanSamples", ctypes.c_uint64), ("bvhNodes", ctypes.c_uint32),
                 ("bvhLeaves", ctypes.c_uint32), ("bvh8Nodes", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32),
-                ("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32)]
+                ("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32),
+                ("traversalStackOverflows", ctypes.c_uint64), ("traversalBudgetExhausted", ctypes.c_uint64),
+                ("bvh8Levels", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
 
 
 class KernelTimes(ctypes.Structure):
-    _fields_ = [("ms", ctypes.c_double * 7), ("launches", ctypes.c_uint64 * 7), ("extensionRays", ctypes.c_uint64),
+    _fields_ = [("ms", ctypes.c_double * 8), ("launches", ctypes.c_uint64 * 8), ("extensionRays", ctypes.c_uint64),
                 ("shadowRays", ctypes.c_uint64)]
 
 

@@ -25,6 +25,13 @@ struct BvhNode {
 
 #define TRI_FLAG_ALPHA 1u  // material needs the alpha (any-hit) test
 
+// Nodes one ray may visit before its walk is cut short (and counted as a
+// fault): more than 2n, the most a walk of a valid BVH2 of n < 2^25
+// triangles visits.
+#define TRAV_DEFAULT_BUDGET (1 << 26)
+// Entries of a ray's BVH8 node-group stack; the build refuses deeper trees.
+#define BVH8_STACK 64
+
 // Per-ray constants of the watertight test (Woop, Benthin, Wald, "Watertight
 // Ray/Triangle Intersection", JCGT 2(1), 2013).
 struct RayPre {

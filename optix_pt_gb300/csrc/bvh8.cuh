@@ -24,7 +24,6 @@ struct Bvh8Node {
     uint4 qx, qy, qz;
 };
 
-#define BVH8_STACK 64
 #ifndef TRAV8_REFILL
 #define TRAV8_REFILL 8  // idle lanes that trigger a refill of a persistent warp
 #endif
@@ -85,7 +84,7 @@ struct Trav8 {
     uint2 grp;
     uint2 stack[BVH8_STACK];
 
-    OPT_D void init(float3 ro, float3 d, float rtmin, float rtmax, HitRec &hit)
+    OPT_D void init(float3 ro, float3 d, float rtmin, float rtmax, HitRec &hit, int nodeBudget)
     {
         hit.leaf = -1;
         pre = rayPrepare(ro, d);
@@ -97,7 +96,7 @@ struct Trav8 {
         node = 0;
         sp = 0;
         bestPrim = INT_MAX;
-        budget = 1 << 24;
+        budget = nodeBudget;
         grp = make_uint2(0u, 0u);
     }
 
@@ -105,8 +104,10 @@ struct Trav8 {
     OPT_D bool step(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, HitRec &hit, AlphaFn &alpha,
                     Counter &ctr)
     {
-        if (--budget < 0)
+        if (--budget < 0) {
+            hit.leaf = HIT_CUT_SHORT;  // a miss that the kernel counts as a fault
             return true;
+        }
         ctr.node();
         const Bvh8Node *N = nodes + node;
         const float4 a = __ldg(&N->a);
@@ -179,6 +180,9 @@ struct Trav8 {
             }
         }
         if (ihits) {
+            // The stack holds at most one group per tree level below the
+            // root, and the build refuses trees deeper than BVH8_STACK
+            // levels, so the bound never drops a group.
             if ((grp.y >> 8) && sp < BVH8_STACK)
                 stack[sp++] = grp;
             grp = make_uint2(b.x, (ihits << 8) | imask);
@@ -200,15 +204,15 @@ struct Trav8 {
     }
 };
 
-template <bool ANY, class AlphaFn, class Counter = NoCount>
+template <bool ANY, class AlphaFn, class Counter>
 OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, float3 o, float3 d,
-                     float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &&ctr = Counter())
+                     float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &ctr, int budget)
 {
     hit.leaf = -1;
     if (nodes == nullptr)
         return false;
     Trav8 T;
-    T.init(o, d, tmin, tmax, hit);
+    T.init(o, d, tmin, tmax, hit, budget);
     while (!T.step<ANY>(nodes, triV, hit, alpha, ctr)) {
     }
     return hit.leaf >= 0;
@@ -224,7 +228,7 @@ OPT_D bool traverse8(const Bvh8Node *__restrict__ nodes, const float4 *__restric
 // parameters); finish(i, hit) stores ray i's result.
 template <bool ANY, class Fetch, class Finish, class AlphaFn, class Counter>
 OPT_D void traverse8Queue(const Bvh8Node *__restrict__ nodes, const float4 *__restrict__ triV, uint32_t count,
-                          uint32_t *next, Fetch fetch, Finish finish, AlphaFn alpha, Counter &ctr)
+                          uint32_t *next, Fetch fetch, Finish finish, AlphaFn alpha, Counter &ctr, int budget)
 {
     const uint32_t lane = threadIdx.x & 31u;
     // The first 32 rays of every warp come in queue order without the
@@ -261,7 +265,7 @@ OPT_D void traverse8Queue(const Bvh8Node *__restrict__ nodes, const float4 *__re
                     float3 o, d;
                     float tmin, tmax;
                     fetch(i, o, d, tmin, tmax, alpha);
-                    T.init(o, d, tmin, tmax, hit);
+                    T.init(o, d, tmin, tmax, hit, budget);
                     ray = (int)i;
                 } else {
                     exhausted = true;

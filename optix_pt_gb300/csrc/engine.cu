@@ -106,6 +106,9 @@ struct optpt_renderer {
     // learned guiding (mode 0 off, 1 guided + online training, 2 guided, frozen)
     optpt_guide *guide = nullptr;
     int guideMode = 0;
+    // First bounce finished by the path-completion kernel (plain sampling);
+    // 0 = every bounce by the per-bounce kernels.
+    uint32_t tailBounce = 0;
     void *gMix = nullptr;        // 80 B per path slot
     float4 *gRec = nullptr;      // GUIDE_REC float4 per (training path, depth)
     void *gBatch = nullptr;      // GuideSample per slot
@@ -381,6 +384,7 @@ int allocFrame(optpt_renderer *r, uint32_t width, uint32_t height)
     r->shape.gridShade = occupancyGrid(2, blk);
     r->shape.gridShadow = occupancyGrid(wide ? 3 : 13, blk);
     r->shape.gridAccum = occupancyGrid(4, blk);
+    r->shape.gridFinish = occupancyGrid(wide ? 5 : 15, 128);
     r->graphDirty = true;
     return OPTPT_OK;
 }
@@ -411,7 +415,17 @@ int enqueuePassOn(optpt_renderer *r, const FrameParams &fp, const WaveBufs &q, c
     const bool fork = ev == nullptr && !count && r->sideStream != nullptr;
     mark(0);
     launchGenerate(r->shape, fp, q, st);
+    // From bounce tailBounce on (plain sampling), one launch finishes every
+    // remaining path (launchFinish) instead of a launch per kernel per bounce.
+    const uint32_t tail = fp.guide.on ? 0u : r->tailBounce;
     for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
+        if (d == tail) {
+            if (fork && d > 1)
+                cudaStreamWaitEvent(st, r->evJoin, 0);  // bounce d - 1's shadow rays resolved
+            mark(7);
+            launchFinish(r->shape, r->scene, fp, q, (int)d, st, count);
+            break;
+        }
         mark(1);
         launchExtend(r->shape, r->scene, fp, q, (int)d, st, count);
         if (fp.guide.on && d < fp.maxDepth && d <= fp.guide.maxDepth) {
@@ -697,6 +711,8 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         r->opt.useGraph = 1;
     if (r->opt.bvhWidth == 0)
         r->opt.bvhWidth = 8;
+    r->tailBounce = r->opt.tailBounce == 0 ? OPTPT_DEFAULT_TAIL_BOUNCE
+                                           : (r->opt.tailBounce == 0xFFFFFFFFu ? 0u : r->opt.tailBounce);
     if (r->opt.bvhWidth != 2 && r->opt.bvhWidth != 8) {
         delete r;
         return fail(OPTPT_ERR_INVALID, "bvhWidth must be 2 or 8");
@@ -814,6 +830,13 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
             rc = cudaFail((cudaError_t)be, "BVH8 collapse");
             break;
         }
+        // A ray's node-group stack holds at most one group per level below
+        // the root: a tree of at most BVH8_STACK levels cannot overflow it.
+        if (r->bvh.nodes8 && r->bvh.levels8 > BVH8_STACK) {
+            rc = fail(OPTPT_ERR_INVALID, "BVH8 of " + std::to_string(r->bvh.levels8) + " levels exceeds the " +
+                                             std::to_string(BVH8_STACK) + "-entry traversal stack");
+            break;
+        }
         DevScene &ds = r->scene;
         ds.nodes = r->bvh.nodes;
         ds.nodes8 = r->bvh.nodes8;
@@ -832,9 +855,10 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         ds.numTris = (int)nt;
         ds.numLights = r->numLights;
         ds.numEmissive = r->numEmissive;
+        ds.nodeBudget = r->opt.nodeBudget ? (int)std::min<uint32_t>(r->opt.nodeBudget, INT_MAX) : TRAV_DEFAULT_BUDGET;
         if ((e = cudaMalloc((void **)&r->q.counters, sizeof(uint32_t) * CNT_TOTAL)) ||
-            (e = cudaMalloc((void **)&r->q.totals, sizeof(unsigned long long) * 8)) ||
-            (e = cudaMemset(r->q.totals, 0, sizeof(unsigned long long) * 8)) ||
+            (e = cudaMalloc((void **)&r->q.totals, sizeof(unsigned long long) * TOTALS_COUNT)) ||
+            (e = cudaMemset(r->q.totals, 0, sizeof(unsigned long long) * TOTALS_COUNT)) ||
             (e = cudaMalloc((void **)&r->dState, sizeof(uint32_t) * 4)) ||
             (e = cudaMemset(r->dState, 0, sizeof(uint32_t) * 4)) ||
             (e = cudaMalloc((void **)&r->dFrameConst, sizeof(FrameConst)))) {
@@ -899,6 +923,7 @@ int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numV
         r->shape.gridShade = occupancyGrid(2, blk);
         r->shape.gridShadow = occupancyGrid(wide ? 3 : 13, blk);
         r->shape.gridAccum = occupancyGrid(4, blk);
+        r->shape.gridFinish = occupancyGrid(wide ? 5 : 15, 128);
     }
     // (Re)allocate when the pixel layout changes; paths per pass: at least one
     // sample for every pixel, and about 2^21 paths when fewer pixels are active.
@@ -1691,13 +1716,16 @@ int optpt_get_stats(optpt_renderer *r, optpt_stats *out)
 {
     if (!r || !out)
         return fail(OPTPT_ERR_INVALID, "NULL argument");
-    unsigned long long t[4] = {0, 0, 0, 0};
+    unsigned long long t[TOTALS_COUNT] = {};
     CUDA_OR_RETURN(cudaDeviceSynchronize(), "stats");
     CUDA_OR_RETURN(cudaMemcpy(t, r->q.totals, sizeof(t), cudaMemcpyDeviceToHost), "stats");
     out->extensionRays = t[0];
     out->shadowRays = t[1];
     out->pathSamples = t[2];
     out->nanSamples = t[3];
+    out->traversalStackOverflows = t[8];
+    out->traversalBudgetExhausted = t[9];
+    out->bvh8Levels = (uint32_t)r->bvh.levels8;
     out->bvhNodes = (uint32_t)r->bvh.usedNodes;
     out->bvhLeaves = (uint32_t)r->bvh.numLeaves;
     out->bvh8Nodes = (uint32_t)r->bvh.numNodes8;
@@ -1808,7 +1836,7 @@ int optpt_trace(optpt_renderer *r, const float *rays, float *hits, uint32_t n, i
         CUDA_OR_RETURN(cudaStreamSynchronize((cudaStream_t)stream), "trace");
         return OPTPT_OK;
     }
-    launchTrace(r->scene, (const float4 *)rays, (float4 *)hits, n, anyHit, (cudaStream_t)stream);
+    launchTrace(r->scene, (const float4 *)rays, (float4 *)hits, n, anyHit, r->q.totals, (cudaStream_t)stream);
     CUDA_OR_RETURN(cudaGetLastError(), "trace launch");
     return OPTPT_OK;
 }

@@ -47,6 +47,7 @@ struct DevScene {
     int numTris;
     int numLights;
     int numEmissive;
+    int nodeBudget;  // BVH nodes one ray may visit; a walk cut short there is counted as a fault
 };
 
 // Per-frame constants, device resident and uploaded before every render (the
@@ -152,6 +153,7 @@ __device__ __forceinline__ uint32_t passPaths(const FrameParams &fp)
 #define CNT_FETCH_EXT 192
 #define CNT_TOTAL 256
 #define OPT_MAX_DEPTH 62
+#define TOTALS_COUNT 10  // entries of WaveBufs::totals
 
 // Wavefront buffers (SoA; P = numPaths):
 //   pathT/pathL : float4 per path (throughput + flags, radiance)
@@ -166,7 +168,8 @@ struct WaveBufs {
     float4 *shO[2], *shD[2], *shC[2];
     uint32_t *counters;              // CNT_TOTAL entries
     unsigned long long *totals;      // 0 ext rays, 1 shadow rays, 2 samples, 3 NaN samples,
-                                     // 4-5 ext nodes/tris, 6-7 shadow nodes/tris (counting mode)
+                                     // 4-5 ext nodes/tris, 6-7 shadow nodes/tris (counting mode),
+                                     // 8 traversal stack overflows, 9 walks cut short by the node budget
 };
 
 // FP64 per-pixel accumulator (xyz used), 32-byte aligned for vector access.
@@ -180,7 +183,7 @@ struct AccumBufs {
 };
 
 struct LaunchShape {
-    int gridGenerate, gridExtend, gridShade, gridShadow, gridAccum;
+    int gridGenerate, gridExtend, gridShade, gridShadow, gridAccum, gridFinish;
     int block;
     int compaction;  // shading-queue appends: 0 one atomic per warp, 1 one per block
 };
@@ -195,10 +198,17 @@ void launchShade(const LaunchShape &ls, const DevScene &s, const FrameParams &fp
                  cudaStream_t st);
 void launchShadow(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth,
                   int which, cudaStream_t st, bool count = false);
+// The rest of every path from bounce depth0 on, in one launch (plain
+// sampling; 128-thread blocks): closest hit, shading and shadow rays per
+// bounce, bit-identical to the per-bounce kernels.
+void launchFinish(const LaunchShape &ls, const DevScene &s, const FrameParams &fp, const WaveBufs &q, int depth0,
+                  cudaStream_t st, bool count = false);
 void launchAccumulate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs &q, const AccumBufs &a,
                       cudaStream_t st);
 void launchAdvance(const FrameParams &fp, uint32_t *state, cudaStream_t st);
-void launchTrace(const DevScene &s, const float4 *rays, float4 *hits, uint32_t n, int anyHit, cudaStream_t st);
+// Traversal faults of the traced rays are added to totals[8], totals[9].
+void launchTrace(const DevScene &s, const float4 *rays, float4 *hits, uint32_t n, int anyHit,
+                 unsigned long long *totals, cudaStream_t st);
 void launchBsdfBatch(const void *queries, void *results, uint32_t n, cudaStream_t st);
 // guide.cu: inference over the extension queue of `depth` (after extend), and
 // the end-of-pass gather of training samples from the records.

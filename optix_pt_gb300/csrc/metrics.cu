@@ -70,30 +70,42 @@ __global__ void __launch_bounds__(RELMSE_BLOCK)
 
 }  // namespace
 
-// Launches both kernels with caller-chosen scratch (tiles doubles).
+// Tiles of an image, in 64 bits: no pixel count can wrap it.
+uint64_t relmseTiles(uint32_t numPixels) { return ((uint64_t)numPixels + RELMSE_TILE - 1) / RELMSE_TILE; }
+
+// Launches both kernels with caller-chosen scratch (relmseTiles doubles).
+// Returns 0 or the CUDA error of these two launches. An error left pending by
+// earlier, unrelated work on this thread is reported as such, without
+// launching and without clearing it, so it is not blamed on this call.
 int relmseLaunch(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
                  double *scratch, cudaStream_t st)
 {
-    const uint32_t tiles = (numPixels + RELMSE_TILE - 1) / RELMSE_TILE;
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+        return optpt_internal_set_error(OPTPT_ERR_CUDA, (std::string("relMSE not launched: an earlier CUDA error is "
+                                                                     "pending: ") + cudaGetErrorString(pending)).c_str());
+    // at most 2^21 tiles for a 32-bit pixel count, within the grid limit
+    const uint32_t tiles = (uint32_t)relmseTiles(numPixels);
     kRelMseTiles<<<tiles, RELMSE_BLOCK, 0, st>>>(reinterpret_cast<const Acc4 *>(sum), 1.0 / (double)nSamples,
                                                  reinterpret_cast<const Acc4 *>(ref), numPixels, scratch);
     kRelMseFinal<<<1, RELMSE_BLOCK, 0, st>>>(scratch, tiles, numPixels, out);
-    return (int)cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return optpt_internal_set_error(OPTPT_ERR_CUDA, (std::string("relMSE launch: ") + cudaGetErrorString(e)).c_str());
+    return OPTPT_OK;
 }
-
-uint32_t relmseTiles(uint32_t numPixels) { return (numPixels + RELMSE_TILE - 1) / RELMSE_TILE; }
 
 // ------------------------------------------------------------------ allocation-free variant
 //
 // For callers that must not allocate device memory at the point of the call:
-// code inside a CUDA stream capture (cudaMalloc is not allowed there, and a
-// stream-ordered allocation would become part of the graph), real-time frame
-// loops that forbid allocator calls, and hosts whose memory pool owns all
-// device memory. The partial sums live in a fixed array in the library's own
-// device memory instead. It holds RELMSE_NOALLOC_TILES tiles, so images of up
-// to RELMSE_NOALLOC_TILES * 2048 = 8,388,608 pixels (a 3840x2160 frame fits);
-// larger images are rejected. Every GPU that loads the library keeps these
-// 32 KiB until the process exits.
+// a progressive viewer's per-frame loop that promises no allocator call per
+// frame (cudaMalloc and cudaFree can synchronise the device and stall the
+// frame), and host applications whose own memory pool owns all device memory
+// and does not let a library allocate behind its back. The partial sums live
+// in a fixed array in the library's own device memory instead. It holds
+// RELMSE_NOALLOC_TILES tiles, so images of up to RELMSE_NOALLOC_TILES * 2048 =
+// 8,388,608 pixels (a 3840x2160 frame fits); larger images are rejected.
+// Every GPU that loads the library keeps these 32 KiB until the process exits.
 constexpr uint32_t RELMSE_NOALLOC_TILES = 4096;
 static __device__ __align__(256) double g_relmseScratch[RELMSE_NOALLOC_TILES];
 
@@ -103,7 +115,11 @@ std::mutex g_scratchMutex;
 double *g_scratchAddr[MAX_DEVICES] = {};  // device address of g_relmseScratch, per device
 
 // Looks up (once per device, with that device current) the device address of
-// the scratch array; host code cannot use the symbol itself as a pointer.
+// the scratch array; host code cannot use the symbol itself as a pointer. The
+// address is cached for the life of the process: a cudaDeviceReset (or any
+// reset of the primary context) unloads the module and makes it stale, so a
+// process that resets a device must not call optpt_relmse_noalloc on it
+// afterwards.
 int scratchAddress(double **out)
 {
     int dev = 0;
@@ -131,7 +147,7 @@ extern "C" int optpt_relmse_noalloc(const double *sum, uint32_t nSamples, const 
 {
     if (!sum || !ref || !out || numPixels == 0 || nSamples == 0)
         return optpt_internal_set_error(OPTPT_ERR_INVALID, "optpt_relmse_noalloc: NULL buffer or empty image");
-    if (relmseTiles(numPixels) > RELMSE_NOALLOC_TILES)
+    if ((uint64_t)numPixels > (uint64_t)RELMSE_NOALLOC_TILES * RELMSE_TILE)
         return optpt_internal_set_error(
             OPTPT_ERR_INVALID,
             ("optpt_relmse_noalloc: " + std::to_string(numPixels) + " pixels exceed the maximum of " +
@@ -144,10 +160,7 @@ extern "C" int optpt_relmse_noalloc(const double *sum, uint32_t nSamples, const 
     // Every tile the final kernel reads is written by the first kernel of the
     // same call, so no clearing is needed; calls that overlap on the GPU
     // share the array and race.
-    rc = relmseLaunch(sum, nSamples, ref, numPixels, out, scratch, (cudaStream_t)stream);
-    if (rc)
-        return optpt_internal_set_error(OPTPT_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
-    return OPTPT_OK;
+    return relmseLaunch(sum, nSamples, ref, numPixels, out, scratch, (cudaStream_t)stream);
 }
 
 extern "C" int optpt_relmse(const double *sum, uint32_t nSamples, const double *ref, uint32_t numPixels, double *out,
@@ -160,9 +173,7 @@ extern "C" int optpt_relmse(const double *sum, uint32_t nSamples, const double *
     cudaError_t e = cudaMallocAsync((void **)&scratch, sizeof(double) * relmseTiles(numPixels), st);
     if (e != cudaSuccess)
         return optpt_internal_set_error(OPTPT_ERR_NOMEM, (std::string("optpt_relmse scratch: ") + cudaGetErrorString(e)).c_str());
-    int rc = relmseLaunch(sum, nSamples, ref, numPixels, out, scratch, st);
+    const int rc = relmseLaunch(sum, nSamples, ref, numPixels, out, scratch, st);
     cudaFreeAsync(scratch, st);
-    if (rc)
-        return optpt_internal_set_error(OPTPT_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
-    return OPTPT_OK;
+    return rc;
 }

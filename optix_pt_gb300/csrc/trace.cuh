@@ -38,6 +38,8 @@ OPT_D float boxEntry(float lox, float hix, float loy, float hiy, float loz, floa
 // Walks the BVH. ANY = true stops at the first accepted hit (occlusion).
 // `alpha(leaf, prim, u, v)` decides whether a candidate on a triangle with
 // TRI_FLAG_ALPHA is kept (the any-hit programs' optixIgnoreIntersection).
+//
+// Counters: node() / tri() count BVH work (counting variants only).
 struct NoCount {
     OPT_D void node() {}
     OPT_D void tri() {}
@@ -48,10 +50,23 @@ struct Count {
     OPT_D void tri() { ++tris; }
 };
 
-template <bool ANY, class AlphaFn, class Counter = NoCount>
-OPT_D bool traverse(const BvhNode *__restrict__ nodes, const float4 *__restrict__ triV, float3 o, float3 d,
-                    float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &&ctr = Counter())
+// Traversal faults leave a ray's result possibly wrong, so they are never
+// silent: the walk returns a miss with one of these leaf values, and the
+// kernels count them (renderer totals 8 and 9, optpt_stats).
+#define HIT_STACK_OVERFLOW (-3)  // a node group was dropped: the stack was full
+#define HIT_CUT_SHORT (-2)       // the walk ran out of its node budget
+// Adds a traversal fault of `leaf` (if it is one) to totals[8] / totals[9].
+OPT_D void countFault(int leaf, unsigned long long *totals)
 {
+    if (leaf < -1)
+        atomicAdd(totals + (leaf == HIT_STACK_OVERFLOW ? 8 : 9), 1ull);
+}
+
+template <bool ANY, class AlphaFn, class Counter>
+OPT_D bool traverse(const BvhNode *__restrict__ nodes, const float4 *__restrict__ triV, float3 o, float3 d,
+                    float tmin, float tmax, HitRec &hit, AlphaFn alpha, Counter &ctr, int budget)
+{
+    bool dropped = false;
     hit.leaf = -1;
     if (nodes == nullptr)  // empty scene
         return false;
@@ -63,8 +78,12 @@ OPT_D bool traverse(const BvhNode *__restrict__ nodes, const float4 *__restrict_
     float tcur = tmax;
     int bestPrim = INT_MAX;
     // The node budget bounds the walk even on a corrupted tree (a valid BVH of
-    // n triangles visits at most 2n nodes).
-    for (int budget = 1 << 26; budget > 0; --budget) {
+    // n triangles visits at most 2n nodes); running out of it is a fault.
+    for (;; --budget) {
+        if (budget <= 0) {
+            hit.leaf = HIT_CUT_SHORT;
+            return false;
+        }
         ctr.node();
         const BvhNode *N = nodes + node;
         const float4 a = __ldg(&N->a), b = __ldg(&N->b), c = __ldg(&N->c);
@@ -114,6 +133,8 @@ OPT_D bool traverse(const BvhNode *__restrict__ nodes, const float4 *__restrict_
             const bool leftFirst = tl <= tr;
             if (sp < BVH_STACK)
                 stack[sp++] = leftFirst ? r.y : r.x;
+            else
+                dropped = true;
             node = leftFirst ? r.x : r.y;
         } else if (hl) {
             node = r.x;
@@ -124,6 +145,10 @@ OPT_D bool traverse(const BvhNode *__restrict__ nodes, const float4 *__restrict_
                 break;
             node = stack[--sp];
         }
+    }
+    if (dropped) {
+        hit.leaf = HIT_STACK_OVERFLOW;
+        return false;
     }
     return hit.leaf >= 0;
 }

@@ -742,6 +742,7 @@ template <class R> F3 tof(V3<R> a) { return F3{(float)a.x, (float)a.y, (float)a.
 struct RenderParams {
     uint32_t w, h, seed, sampleBase, spp, maxDepth;
     float eye[3], U[3], V[3], W[3], bg[3];
+    int vis;  // LaunchParams::vis: 0 = path tracing, 1-12 = material visualisation
 };
 
 struct Counters {
@@ -823,15 +824,18 @@ V3<R> tracePath(const SceneView &sv, const RenderParams &rp, uint32_t pixel, uin
         }
         // Material inputs after textures (cu/path_tracer.cu:165-229).
         V3<R> albedo = v3f<R>(M.baseColour);
+        R alpha = R(M.baseColour[3]);
         if (M.hasBaseColourTexture) {
             float c[4];
             tex(M.baseColourTexture, M.baseColourTexTf, c);
             albedo = albedo * v3<R>(R(c[0]), R(c[1]), R(c[2]));
+            alpha *= R(c[3]);
         }
-        R roughness = R(M.roughness), metallic = R(M.metallic);
+        R roughness = R(M.roughness), metallic = R(M.metallic), occlusion = R(1);
         if (M.hasMetallicRoughnessTexture) {
             float c[4];
             tex(M.metallicRoughnessTexture, M.metallicRoughnessTexTf, c);
+            occlusion *= R(c[0]);
             roughness *= R(c[1]);
             metallic = c[2] < 0.04f ? R(0) : metallic * R(c[2]);
         }
@@ -858,6 +862,23 @@ V3<R> tracePath(const SceneView &sv, const RenderParams &rp, uint32_t pixel, uin
         R cw;
         const uint32_t cat =
             categorise(mc, -rayDir, normal, roughness, metallic, emission, sheenColour, sheenRoughness, U, cw);
+        if (rp.vis != 0) {  // material visualisation: the path ends here (cu/path_tracer.cu:252-315)
+            switch (rp.vis) {
+            case 1: L = v3s<R>(metallic); break;
+            case 2: L = v3s<R>(roughness); break;
+            case 3: L = v3s<R>(occlusion); break;
+            case 4: L = emission; break;
+            case 5: L = normal * R(0.5f) + v3s<R>(R(0.5f)); break;
+            case 6: L = Ng * R(0.5f) + v3s<R>(R(0.5f)); break;
+            case 7: L = albedo; break;
+            case 8: L = metallic * albedo * v3s<R>(R(M.specular)); break;  // "glossy colour"
+            case 10: L = sheenColour; break;
+            case 11: L = v3s<R>(sheenRoughness); break;
+            case 12: L = v3s<R>(alpha); break;
+            default: break;  // 9 (specular colour) is unfinished in the reference: radiance unchanged
+            }
+            break;
+        }
         const bool spec = (cat & Specular) != 0;
         if (!spec)
             hitPoint = hitPoint - rayDir * R(0.001f);
@@ -1119,7 +1140,7 @@ int orc_trace(void *view, const float *rays, float *hits, uint32_t n, int anyHit
 // nodes visited, triangle tests.
 int orc_render(void *view, const float *camera /* eye U V W bg: 15 floats */, uint32_t w, uint32_t h, uint32_t seed,
                uint32_t sampleBase, uint32_t spp, uint32_t maxDepth, uint32_t y0, uint32_t y1, int precision,
-               int threads, double *sum, double *sumSq, uint64_t *counters)
+               int threads, double *sum, double *sumSq, uint64_t *counters, int vis)
 {
     const SceneView &sv = *(SceneView *)view;
     RenderParams rp{};
@@ -1129,6 +1150,7 @@ int orc_render(void *view, const float *camera /* eye U V W bg: 15 floats */, ui
     rp.sampleBase = sampleBase;
     rp.spp = spp;
     rp.maxDepth = maxDepth;
+    rp.vis = vis;
     memcpy(rp.eye, camera, 12);
     memcpy(rp.U, camera + 3, 12);
     memcpy(rp.V, camera + 6, 12);

@@ -30,3 +30,34 @@ def cuda_dev(built):
         pytest.skip("no CUDA device")
     torch.cuda.set_device(0)
     return torch.device("cuda:0")
+
+
+@pytest.fixture(autouse=True)
+def no_traversal_faults(request):
+    """Every renderer a GPU test closes (or drops) must report zero traversal
+    faults: no node group dropped from a full stack, no walk cut short by the
+    node budget. A test that provokes faults on purpose marks its renderer
+    with `expect_traversal_faults = True`."""
+    if request.node.get_closest_marker("gpu") is None:
+        yield
+        return
+    import gc
+
+    import optix_pt_gb300 as opt
+    faults = []
+    orig_close = opt.Renderer.close
+
+    def checked_close(self):
+        if getattr(self, "_h", None) and not getattr(self, "expect_traversal_faults", False):
+            st = self.stats()
+            if st["traversalStackOverflows"] or st["traversalBudgetExhausted"]:
+                faults.append((st["traversalStackOverflows"], st["traversalBudgetExhausted"]))
+        orig_close(self)
+
+    opt.Renderer.close = checked_close
+    try:
+        yield
+        gc.collect()
+    finally:
+        opt.Renderer.close = orig_close
+    assert not faults, "traversal faults (stack overflows, walks cut short): %s" % faults

@@ -128,3 +128,30 @@ FP32_ENVELOPE = {
 def within(metrics, envelope=FP32_ENVELOPE):
     bad = {k: v for k, v in metrics.items() if v[0] > envelope[k][0] or v[1] > envelope[k][1]}
     return not bad, bad
+
+
+# ---------------------------------------------------------------- FP32 against FP64, query by query
+FIELDS = ("f", "pdf", "bsdf", "dir")
+
+
+def rel_error(x, y):
+    """Norm-relative error |x - y| / |y| of each query's vector (or scalar)
+    field; 0 where both are zero, inf where only y is zero or either is NaN."""
+    x = np.asarray(x, np.float64).reshape(len(x), -1)
+    y = np.asarray(y, np.float64).reshape(len(y), -1)
+    d = np.linalg.norm(x - y, axis=1)
+    den = np.linalg.norm(y, axis=1)
+    r = np.where(den > 0, d / np.where(den > 0, den, 1.0), np.where(d > 0, np.inf, 0.0))
+    return np.nan_to_num(r, nan=np.inf)
+
+
+def ulp_distance(x, y):
+    """Largest distance in FP32 units in the last place over a query's
+    components (0 = bit-identical; NaN pairs count as identical)."""
+    def key(v):
+        b = np.asarray(v, np.float32).reshape(len(v), -1).view(np.int32).astype(np.int64)
+        return np.where(b < 0, -(b & 0x7FFFFFFF), b)
+    a, b = key(x), key(y)
+    both_nan = np.isnan(np.asarray(x, np.float32).reshape(len(x), -1)) & \
+        np.isnan(np.asarray(y, np.float32).reshape(len(y), -1))
+    return np.where(both_nan, 0, np.abs(a - b)).max(1)

@@ -111,10 +111,13 @@ def soup(n, seed, dup=False, scale=0.15):
     return P, I
 
 
-def render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None, **renderer_kw):
+def render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None, classify=False, **renderer_kw):
     """GPU render (sample indices from 0) and an oracle render of the same
     frame (sample indices from cpu_base): ((sum, sumsq, n) GPU, (sum, sumsq,
-    n) oracle, GPU stats, oracle ray counts)."""
+    n) oracle, GPU stats, oracle ray counts). classify=True appends a fifth
+    item, the same oracle render from the oracle's build with fused
+    multiply-adds (a second FP32 rounding of the same paths), for
+    paired_agreement."""
     import torch
 
     import optix_pt_gb300 as opt
@@ -130,7 +133,26 @@ def render_pair(scene, w, h, spp_gpu, spp_cpu, cpu_base, precision, batch=None, 
     cs, cq, cnt = v.render(cam, w, h, lp.seed, cpu_base, spp_cpu, lp.maxDepth, precision=precision)
     st = r.stats()
     r.close()
-    return (s.reshape(-1, 3), q.reshape(-1, 3), n), (cs, cq, spp_cpu), st, cnt
+    out = (s.reshape(-1, 3), q.reshape(-1, 3), n), (cs, cq, spp_cpu), st, cnt
+    if classify:
+        vf = orc.SceneView(scene.struct, 4, variant="fma")
+        fs, fq, _ = vf.render(cam, w, h, lp.seed, cpu_base, spp_cpu, lp.maxDepth, precision=precision)
+        out = out + ((fs, fq, spp_cpu),)
+    return out
+
+
+def paired_agreement(g, c, f, rtol=1e-4, atol=1e-5):
+    """Pixels of a paired render (same random streams) on which the GPU and
+    the FP32 oracle agree, split by whether the path is robust to FP32
+    rounding: a pixel is rounding-sensitive when the oracle's two FP32 builds
+    (without and with fused multiply-adds) already disagree on it. Returns
+    (agreement on robust pixels, fraction of rounding-sensitive pixels,
+    agreement on all pixels)."""
+    def close(a, b):
+        return (np.abs(a - b) <= rtol * np.maximum(1.0, np.abs(b)) + atol).all(1)
+    robust = close(f[0], c[0])
+    agree = close(g[0], c[0])
+    return float(agree[robust].mean()), float(1.0 - robust.mean()), float(agree.mean())
 
 
 def pixel_stats(g, c):

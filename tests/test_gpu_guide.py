@@ -112,7 +112,7 @@ def test_guide_inference_matches_oracle(cuda_dev):
     p_ref = (wr * go.vmf_pdf(mur, kapr, dirs)[0]).sum(1)
     rel = np.abs(p_gpu - p_ref) / p_ref
     print("mixture pdf rel err: median %.2e p99 %.2e max %.2e" % (np.median(rel), np.quantile(rel, 0.99), rel.max()))
-    assert np.median(rel) < 1e-3 and np.quantile(rel, 0.99) < 5e-3
+    assert np.median(rel) <= 1e-4 and np.quantile(rel, 0.99) <= 5e-4
     assert np.abs(w - wr).max() < 1e-2
     assert np.abs(go.unpack_select(out.cpu().numpy()) - go.select_prob(o)).max() < 2e-3
     g.close()
@@ -136,11 +136,11 @@ def test_guide_gradients_match_oracle(cuda_dev):
     for l in range(5):
         err = np.linalg.norm(dm[l] - rdm[l]) / np.linalg.norm(rdm[l])
         print("layer %d dW rel err %.2e" % (l, err))
-        assert err < 5e-3, (l, err)
+        assert err <= 2e-4, (l, err)
     touched = rdh != 0
     err = np.linalg.norm(dh[touched] - rdh[touched]) / np.linalg.norm(rdh[touched])
     print("hash grad rel err %.2e over %d entries; untouched max %.1e" % (err, touched.sum(), np.abs(dh[~touched]).max()))
-    assert err < 5e-3
+    assert err <= 2e-4
     assert np.abs(dh[~touched]).max() == 0.0
     g.close()
 

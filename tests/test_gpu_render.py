@@ -9,7 +9,7 @@
 import numpy as np
 import pytest
 
-from gpu_util import ArrayScene, material, pixel_stats, render_pair
+from gpu_util import ArrayScene, material, paired_agreement, pixel_stats, render_pair
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
@@ -26,13 +26,18 @@ _stats = pixel_stats
 
 @pytest.mark.parametrize("name,w,h,spp", [("cornell", 96, 96, 1), ("cornell", 96, 96, 4), ("spheres", 160, 90, 2)])
 def test_paired_samples_follow_oracle_paths(cuda_dev, name, w, h, spp):
+    """Same random streams on both sides: the GPU follows the FP32 oracle's
+    path to 1e-4 in at least 99.5% of the pixels whose result is robust to
+    FP32 rounding; the others are the pixels on which the oracle's own two
+    FP32 builds (without / with fused multiply-adds) already disagree."""
     import optix_pt_gb300 as opt
     sc = opt.Scene.procedural(name)
-    g, c, st, cnt = _render_pair(sc, w, h, spp, spp, 0, 32, batch=spp)
-    gl, cl = g[0], c[0]
-    close = np.abs(gl - cl) <= 1e-4 * np.maximum(1.0, np.abs(cl)) + 1e-5
-    frac = close.all(1).mean()
-    assert frac > 0.97, frac
+    g, c, st, cnt, f = _render_pair(sc, w, h, spp, spp, 0, 32, batch=spp, classify=True)
+    robust, sensitive, overall = paired_agreement(g, c, f)
+    print("%s %dx%d %d spp: robust-pixel agreement %.4f, rounding-sensitive pixels %.4f, all pixels %.4f" % (
+        name, w, h, spp, robust, sensitive, overall))
+    assert robust >= 0.995, robust
+    assert sensitive <= 0.05, sensitive
     assert abs(int(st["extensionRays"]) - int(cnt[0])) <= 0.02 * int(cnt[0])
     assert abs(int(st["shadowRays"]) - int(cnt[1])) <= 0.02 * max(1, int(cnt[1]))
 

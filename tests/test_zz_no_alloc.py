@@ -1,10 +1,13 @@
 """The allocation-free relMSE entry point, called through the C ABI.
 
 optpt_relmse_noalloc serves callers that cannot allocate device memory when
-they call it (inside a stream capture, in allocation-free frame loops, or under
-a host-owned memory pool). It must give the same result as optpt_relmse, on
-consecutive calls that reuse its fixed scratch array, and refuse images larger
-than that array covers. This file is collected last on purpose.
+they call it: a viewer's frame loop that makes no allocator call per frame
+(cudaMalloc and cudaFree can synchronise the device), or a host whose own
+memory pool owns the device memory. It must give the same result as
+optpt_relmse, on consecutive calls that reuse its fixed scratch array, up to
+and including the largest image that array covers, and refuse larger images.
+This file is collected last on purpose: if it fails, a run that stops at the
+first failure has already run every other test.
 """
 import ctypes
 
@@ -58,6 +61,37 @@ def test_noalloc_rejects_images_beyond_its_scratch(cuda_dev):
     rc = lib.optpt_relmse_noalloc(p, 1, p, 8_388_609, p, None)   # rejected before any device work
     assert rc == -1
     assert b"8388608" in lib.optpt_last_error()
-    rc = lib.optpt_relmse_noalloc(p, 1, p, 1, p, None)          # the largest-but-one case is fine
+    for npix in (4_294_967_295, 4_294_965_249):                   # would wrap a 32-bit tile count
+        assert lib.optpt_relmse_noalloc(p, 1, p, npix, p, None) == -1
+    rc = lib.optpt_relmse_noalloc(p, 1, p, 1, p, None)          # a one-pixel image is fine
     torch.cuda.synchronize()
     assert rc == 0
+
+
+def test_noalloc_at_its_exact_limit(cuda_dev):
+    """8,388,608 pixels: every one of the 4,096 scratch entries is written and
+    read; the result equals the allocating entry point's, twice in a row."""
+    import torch
+
+    from optix_pt_gb300 import _ffi
+    lib = _ffi.lib
+    npix = 8_388_608
+    g = torch.Generator(device=cuda_dev).manual_seed(5)
+    out = torch.zeros(4, dtype=torch.float64, device=cuda_dev)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for k, n_samples in enumerate((16, 3)):
+        s = torch.rand((npix, 4), dtype=torch.float64, device=cuda_dev, generator=g) * (2.0 * n_samples)
+        r = torch.rand((npix, 4), dtype=torch.float64, device=cuda_dev, generator=g)
+        rc = lib.optpt_relmse(ctypes.c_void_p(s.data_ptr()), n_samples, ctypes.c_void_p(r.data_ptr()), npix,
+                              ctypes.c_void_p(out.data_ptr() + 16 * k), stream)
+        assert rc == 0, lib.optpt_last_error()
+        rc = lib.optpt_relmse_noalloc(ctypes.c_void_p(s.data_ptr()), n_samples, ctypes.c_void_p(r.data_ptr()), npix,
+                                      ctypes.c_void_p(out.data_ptr() + 16 * k + 8), stream)
+        assert rc == 0, lib.optpt_last_error()
+        torch.cuda.synchronize()
+        i = s[:, :3] / n_samples
+        expect = float((((i - r[:, :3]) ** 2) / (r[:, :3] ** 2 + 1e-2)).sum(1).mean())
+        a, b = out[2 * k].item(), out[2 * k + 1].item()
+        assert b == pytest.approx(a, rel=1e-12)
+        assert b == pytest.approx(expect, rel=1e-12)
+        del s, r
