@@ -365,7 +365,8 @@ typedef struct optpt_stats {
     uint64_t traversalStackOverflows;
     uint64_t traversalBudgetExhausted;
     uint32_t bvh8Levels;     /* levels of the 8-wide BVH (<= 64)                    */
-    uint32_t pad;
+    uint32_t tailBounce;     /* first bounce of plain passes finished by the path-
+                              * completion kernel (0: none)                        */
 } optpt_stats;
 int optpt_get_stats(optpt_renderer *r, optpt_stats *out);
 

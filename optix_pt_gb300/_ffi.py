@@ -121,7 +121,7 @@ class Stats(ctypes.Structure):
                 ("bvhLeaves", ctypes.c_uint32), ("bvh8Nodes", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32),
                 ("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32),
                 ("traversalStackOverflows", ctypes.c_uint64), ("traversalBudgetExhausted", ctypes.c_uint64),
-                ("bvh8Levels", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+                ("bvh8Levels", ctypes.c_uint32), ("tailBounce", ctypes.c_uint32)]
 
 
 class KernelTimes(ctypes.Structure):

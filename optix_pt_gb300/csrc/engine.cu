@@ -1726,6 +1726,7 @@ int optpt_get_stats(optpt_renderer *r, optpt_stats *out)
     out->traversalStackOverflows = t[8];
     out->traversalBudgetExhausted = t[9];
     out->bvh8Levels = (uint32_t)r->bvh.levels8;
+    out->tailBounce = r->tailBounce <= r->lp.maxDepth ? r->tailBounce : 0u;
     out->bvhNodes = (uint32_t)r->bvh.usedNodes;
     out->bvhLeaves = (uint32_t)r->bvh.numLeaves;
     out->bvh8Nodes = (uint32_t)r->bvh.numNodes8;

@@ -26,6 +26,9 @@ OPT_D int wrapTexel(int i, int n, int mode)
     return ((i % n) + n) % n;
 }
 
+// Byte -> [0, 1] as one rounded multiply; __fmul_rn keeps the compiler from
+// fusing it into the filter's differences (a fused multiply-subtract rounds
+// differently from the host's separate operations).
 OPT_D float4 texelToFloat(uint32_t t, bool srgb)
 {
     float4 c;
@@ -34,11 +37,11 @@ OPT_D float4 texelToFloat(uint32_t t, bool srgb)
         c.y = c_srgbToLinear[(t >> 8) & 0xFFu];
         c.z = c_srgbToLinear[(t >> 16) & 0xFFu];
     } else {
-        c.x = (float)(t & 0xFFu) * (1.0f / 255.0f);
-        c.y = (float)((t >> 8) & 0xFFu) * (1.0f / 255.0f);
-        c.z = (float)((t >> 16) & 0xFFu) * (1.0f / 255.0f);
+        c.x = __fmul_rn((float)(t & 0xFFu), 1.0f / 255.0f);
+        c.y = __fmul_rn((float)((t >> 8) & 0xFFu), 1.0f / 255.0f);
+        c.z = __fmul_rn((float)((t >> 16) & 0xFFu), 1.0f / 255.0f);
     }
-    c.w = (float)(t >> 24) * (1.0f / 255.0f);
+    c.w = __fmul_rn((float)(t >> 24), 1.0f / 255.0f);
     return c;
 }
 

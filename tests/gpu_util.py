@@ -170,3 +170,28 @@ def pixel_stats(g, c):
     frac = float((z[live] > 3.0).mean()) if live.any() else 0.0
     se = np.sqrt(var.sum()) / var.size
     return frac, abs(gm.mean() - cm.mean()), se, gm, cm, live
+
+
+def tile_stats(g, c, w, tile=8):
+    """z scores of tile means (tile x tile pixels) of two independent
+    estimates of a frame whose rows are `w` pixels wide: averaging over a
+    tile makes the means closer to Gaussian and their variance estimates
+    steadier than per pixel, so the 3-sigma rate is the one a bias would
+    lift. Returns the fraction of tile channels with z > 3."""
+    (gs, gq, gn), (cs, cq, cn) = g, c
+    gm, cm = gs / gn, cs / cn
+    gv = np.maximum(gq / gn - gm ** 2, 0) / gn
+    cv = np.maximum(cq / cn - cm ** 2, 0) / cn
+    h = gm.shape[0] // w
+    th, tw = h // tile, w // tile
+
+    def tiles(a):
+        a = a.reshape(h, w, 3)[:th * tile, :tw * tile]
+        return a.reshape(th, tile, tw, tile, 3).sum((1, 3))
+
+    n = tile * tile
+    d = (tiles(gm) - tiles(cm)) / n
+    var = (tiles(gv) + tiles(cv)) / (n * n)
+    live = var > 0
+    z = np.abs(d[live]) / np.sqrt(var[live])
+    return float((z > 3.0).mean()) if z.size else 0.0

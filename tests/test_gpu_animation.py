@@ -150,7 +150,7 @@ def test_render_after_deform_follows_oracle(cuda_dev, anim_path):
     robust, sensitive, overall = paired_agreement((g,), (cs,), (fs,))
     print("after deform: robust-pixel agreement %.4f, rounding-sensitive pixels %.4f, all pixels %.4f" % (
         robust, sensitive, overall))
-    assert robust >= 0.995, robust
+    assert robust >= 0.995 and overall >= 0.995, (robust, overall)
     assert sensitive <= 0.05, sensitive
     assert g.sum() > 0
     r.close()

@@ -113,7 +113,7 @@ def test_textured_scene_follows_oracle_paths(cuda_dev, textured):
     robust, sensitive, overall = paired_agreement(g, c, f)
     print("robust-pixel agreement %.4f, rounding-sensitive pixels %.4f, all pixels %.4f" % (
         robust, sensitive, overall))
-    assert robust >= 0.995, robust
+    assert robust >= 0.995 and overall >= 0.995, (robust, overall)
     assert sensitive <= 0.05, sensitive
     assert abs(int(st["extensionRays"]) - int(cnt[0])) <= 0.02 * int(cnt[0])
     assert abs(int(st["shadowRays"]) - int(cnt[1])) <= 0.02 * max(1, int(cnt[1]))

@@ -9,7 +9,7 @@
 import numpy as np
 import pytest
 
-from gpu_util import ArrayScene, material, paired_agreement, pixel_stats, render_pair
+from gpu_util import ArrayScene, material, paired_agreement, pixel_stats, render_pair, tile_stats
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
@@ -36,7 +36,7 @@ def test_paired_samples_follow_oracle_paths(cuda_dev, name, w, h, spp):
     robust, sensitive, overall = paired_agreement(g, c, f)
     print("%s %dx%d %d spp: robust-pixel agreement %.4f, rounding-sensitive pixels %.4f, all pixels %.4f" % (
         name, w, h, spp, robust, sensitive, overall))
-    assert robust >= 0.995, robust
+    assert robust >= 0.995 and overall >= 0.995, (robust, overall)
     assert sensitive <= 0.05, sensitive
     assert abs(int(st["extensionRays"]) - int(cnt[0])) <= 0.02 * int(cnt[0])
     assert abs(int(st["shadowRays"]) - int(cnt[1])) <= 0.02 * max(1, int(cnt[1]))
@@ -55,6 +55,61 @@ def test_unbiased_against_fp64(cuda_dev, name, w, h, spp_gpu, spp_cpu, max_frac)
     assert dmean < 4 * se, (dmean, se)
     rel_mse = float(np.mean((gm - cm) ** 2 / (cm ** 2 + 1e-2)))
     print("%s: z>3 fraction %.4f, mean diff %.3g (SE %.3g), relMSE %.3g" % (name, frac, dmean, se, rel_mse))
+
+
+def _full_size(name, w, h, depth, spp_gpu, spp_cpu, rows):
+    """GPU render of the whole frame at spp_gpu, FP64 oracle render of `rows`
+    rows through the middle at spp_cpu (independent sample indices): per-pixel
+    z scores and relMSE over those rows."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural(name)
+    r = opt.Renderer(sc)
+    r.setupOutputBuffer(w, h)
+    r.set_max_depth(depth)
+    r.render(spp_gpu, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    s, q, n = r.accum()
+    cam, lp = _camera(r)
+    st = r.stats()
+    r.close()
+    y0 = (h - rows) // 2
+    cs, cq, _ = orc.SceneView(sc.struct, 4).render(cam, w, h, lp.seed, 1 << 24, spp_cpu, depth, y0=y0,
+                                                   y1=y0 + rows, precision=64)
+    sl = slice(y0 * w, (y0 + rows) * w)
+    g = (s.reshape(-1, 3)[sl], q.reshape(-1, 3)[sl], n)
+    c = (cs[sl], cq[sl], spp_cpu)
+    frac, dmean, se, gm, cm, live = _stats(g, c)
+    tfrac = tile_stats(g, c, w)
+    rel_mse = float(np.mean((gm - cm) ** 2 / (cm ** 2 + 1e-2)))
+    print("%s %dx%d depth %d: GPU %d spp vs FP64 oracle %d spp on %d rows: z>3 fraction %.4f per pixel, %.4f per "
+          "8x8 tile; mean diff %.3g (SE %.3g), relMSE %.3g" % (name, w, h, depth, spp_gpu, spp_cpu, rows, frac, tfrac,
+                                                            dmean, se, rel_mse))
+    assert st["traversalStackOverflows"] == 0 and st["traversalBudgetExhausted"] == 0
+    return frac, tfrac, dmean, se, rel_mse
+
+
+# Per pixel, radiance is heavy-tailed (rare light paths, Russian roulette
+# weights) and each pixel's variance is estimated from its own samples, so
+# the per-pixel 3-sigma rate sits above the Gaussian 0.27%; 8x8-tile means
+# are close to Gaussian, and their rate is the one a bias would lift.
+def test_cornell_at_its_stated_size_unbiased_against_fp64(cuda_dev):
+    """The Cornell box at 512x512, depth 8: 4,096 spp on the GPU against the
+    FP64 oracle at 256 spp over the whole frame."""
+    frac, tfrac, dmean, se, rel_mse = _full_size("cornell", 512, 512, 8, 4096, 256, 512)
+    assert frac < 0.02, frac
+    assert tfrac < 0.01, tfrac
+    assert dmean < 4 * se, (dmean, se)
+
+
+def test_sweep_at_1080p_unbiased_on_a_crop(cuda_dev):
+    """The material sweep at 1920x1080, depth 12: 1,024 spp on the GPU, the
+    FP64 oracle at 64 spp on the 48 rows through the middle of the frame."""
+    frac, tfrac, dmean, se, rel_mse = _full_size("spheres", 1920, 1080, 12, 1024, 64, 48)
+    assert frac < 0.025, frac
+    assert tfrac < 0.01, tfrac
+    assert dmean < 4 * se, (dmean, se)
 
 
 def test_graph_and_direct_launch_are_identical(cuda_dev):
