@@ -66,7 +66,8 @@ GUIDED = {"workload": "indirect-lit interior (doorway only), 1,947,146 tris, dep
           "guiding_options": {"trainSpp": 1024, "trainStride": 2, "alphaMax": 0.6}}
 BATCH = {"workload": "batched multi-view: 96 views (48 of the terrain, 48 of the material sweep), sides "
                      "log-uniform 128..1024, spp U{16..256}, depth 12, guiding on; one batch per scene, each "
-                     "autotuned (leaf size, block size, compaction)", "views_per_scene": 48, "seed": 5,
+                     "autotuned with guiding on (leaf size, block size, compaction)", "views_per_scene": 48,
+         "seed": 5,
          "reference_spp_factor": 4}
 WORKLOAD = dict(WORKLOADS["sweep"])
 METRIC = "Mrays/s (extension + shadow rays traced), progressive path tracing, 1 spp per step"
@@ -547,7 +548,7 @@ def run_batch(stream, peak):
     rel_all, plain_all = [], []
     for name in ("terrain", "spheres"):
         scene = opt.Scene.procedural(name)
-        best, trials = opt.autotune(scene, 320, 180, 16)
+        best, trials = opt.autotune(scene, 320, 180, 16, guiding=1)   # timed as it renders: guided
         r = opt.Renderer(scene, leaf_size=best["leafSize"], block_size=best["blockSize"],
                          compaction=best["compaction"])
         r.set_max_depth(12)

@@ -489,7 +489,8 @@ int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss, double *la
  * and the shading-queue compaction (per warp, per block) that render the
  * scene fastest (pixel-samples per second) at width x height with `spp`
  * samples timed after `warmupSpp` untimed ones (0 = 2), guiding mode
- * `guiding` (0 plain; see optpt_set_guiding). The reference has no
+ * `guiding` (0 plain; see optpt_set_guiding); then, for plain sampling, the
+ * tailBounce (never, 3, 4, 5, 6, 8) with those choices. The reference has no
  * counterpart: OptiX makes these choices internally. One renderer per
  * candidate; `trials` (optional) receives every measurement. */
 typedef struct optpt_autotune_request {

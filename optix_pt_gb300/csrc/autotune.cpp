@@ -2,8 +2,10 @@
 // and build parameters the reference leaves to OptiX (src/renderer.cpp:
 // 441-513 builds the acceleration structure with OptiX's own choices): the
 // BVH8 leaf size, the wavefront block size and the shading-queue compaction
-// granularity, by timing each candidate on the caller's scene. It is a
-// client of the public C ABI (one renderer per candidate) plus CUDA events.
+// granularity, by timing each candidate on the caller's scene, then (plain
+// sampling) the bounce from which the path-completion kernel takes over,
+// with the chosen parameters. It is a client of the public C ABI (one
+// renderer per candidate) plus CUDA events.
 #include <cuda_runtime.h>
 #include <cstring>
 #include <string>
@@ -109,6 +111,30 @@ extern "C" int optpt_autotune(const optpt_scene *scene, const optpt_autotune_req
                     chosen = o;
                 }
             }
+    if (!req->guiding) {
+        // the path-completion switch: never, or from one of these bounces
+        static const uint32_t tails[] = {0xFFFFFFFFu, 3, 4, 5, 6, 8};
+        const optpt_options base = chosen;
+        for (uint32_t tb : tails) {
+            optpt_options o = base;
+            o.tailBounce = tb;
+            Timed t;
+            int rc = timeCandidate(scene, o, req->width, req->height, req->warmupSpp ? req->warmupSpp : 2, req->spp,
+                                   0, t);
+            if (rc)
+                return rc;
+            if (trials && n < maxTrials) {
+                trials[n].options = o;
+                trials[n].samplesPerS = t.samplesPerS;
+                trials[n].mraysPerS = t.mraysPerS;
+            }
+            ++n;
+            if (t.samplesPerS > bestRate) {
+                bestRate = t.samplesPerS;
+                chosen = o;
+            }
+        }
+    }
     *best = chosen;
     if (numTrials)
         *numTrials = n;
