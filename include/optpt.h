@@ -202,13 +202,15 @@ typedef struct optpt_options {
     uint32_t nodeBudget; /* BVH nodes one ray may visit before its walk is cut short
                           * (0 = 2^26, more than any walk of a valid tree needs); a
                           * cut-short walk is counted in optpt_stats               */
-    uint32_t tailBounce; /* plain sampling: from this bounce on, one launch finishes
-                          * every remaining path (closest hit, shading and shadow
-                          * rays per bounce, bit-identical to the per-bounce
-                          * kernels) instead of a launch per kernel per bounce;
-                          * 0 = OPTPT_DEFAULT_TAIL_BOUNCE, 0xFFFFFFFF = never      */
+    uint32_t tailBounce; /* from this bounce on, one launch finishes every
+                          * remaining path (closest hit, shading and shadow rays
+                          * per bounce, bit-identical to the per-bounce kernels)
+                          * instead of a launch per kernel per bounce; with
+                          * guiding on only if it is past the guided bounces
+                          * (>= guiding maxDepth + 2); 0 =
+                          * OPTPT_DEFAULT_TAIL_BOUNCE, 0xFFFFFFFF = never       */
 } optpt_options;
-#define OPTPT_DEFAULT_TAIL_BOUNCE 3
+#define OPTPT_DEFAULT_TAIL_BOUNCE 5
 
 /* Uploads the scene and builds the BVH on the GPU. Replaces the reference's
  * init sequence Renderer(SceneDesc&) .. loadScene() .. buildAccel(true)

@@ -415,9 +415,16 @@ int enqueuePassOn(optpt_renderer *r, const FrameParams &fp, const WaveBufs &q, c
     const bool fork = ev == nullptr && !count && r->sideStream != nullptr;
     mark(0);
     launchGenerate(r->shape, fp, q, st);
-    // From bounce tailBounce on (plain sampling), one launch finishes every
-    // remaining path (launchFinish) instead of a launch per kernel per bounce.
-    const uint32_t tail = fp.guide.on ? 0u : r->tailBounce;
+    // From bounce tailBounce on, one launch finishes every remaining path
+    // (launchFinish) instead of a launch per kernel per bounce. It samples
+    // the BSDF only, so with guiding on it takes over only past the guided
+    // bounces: from guide.maxDepth + 2 on, since the guided shading of bounce
+    // guide.maxDepth + 1 still writes the arrival record of a training path's
+    // last guided vertex.
+    const uint32_t tail = !fp.guide.on ? r->tailBounce
+                          : (fp.guide.maxDepth < OPT_MAX_DEPTH && r->tailBounce >= fp.guide.maxDepth + 2u
+                                 ? r->tailBounce
+                                 : 0u);
     for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
         if (d == tail) {
             if (fork && d > 1)

@@ -57,7 +57,7 @@ def test_unbiased_against_fp64(cuda_dev, name, w, h, spp_gpu, spp_cpu, max_frac)
     print("%s: z>3 fraction %.4f, mean diff %.3g (SE %.3g), relMSE %.3g" % (name, frac, dmean, se, rel_mse))
 
 
-def _full_size(name, w, h, depth, spp_gpu, spp_cpu, rows):
+def _full_size(name, w, h, depth, spp_gpu, spp_cpu, rows, tile=8):
     """GPU render of the whole frame at spp_gpu, FP64 oracle render of `rows`
     rows through the middle at spp_cpu (independent sample indices): per-pixel
     z scores and relMSE over those rows."""
@@ -81,19 +81,22 @@ def _full_size(name, w, h, depth, spp_gpu, spp_cpu, rows):
     g = (s.reshape(-1, 3)[sl], q.reshape(-1, 3)[sl], n)
     c = (cs[sl], cq[sl], spp_cpu)
     frac, dmean, se, gm, cm, live = _stats(g, c)
-    tfrac = tile_stats(g, c, w)
+    tfrac = tile_stats(g, c, w, tile)
     rel_mse = float(np.mean((gm - cm) ** 2 / (cm ** 2 + 1e-2)))
     print("%s %dx%d depth %d: GPU %d spp vs FP64 oracle %d spp on %d rows: z>3 fraction %.4f per pixel, %.4f per "
-          "8x8 tile; mean diff %.3g (SE %.3g), relMSE %.3g" % (name, w, h, depth, spp_gpu, spp_cpu, rows, frac, tfrac,
-                                                            dmean, se, rel_mse))
+          "%dx%d tile; mean diff %.3g (SE %.3g), relMSE %.3g" % (name, w, h, depth, spp_gpu, spp_cpu, rows, frac, tfrac,
+                                                              tile, tile, dmean, se, rel_mse))
     assert st["traversalStackOverflows"] == 0 and st["traversalBudgetExhausted"] == 0
     return frac, tfrac, dmean, se, rel_mse
 
 
 # Per pixel, radiance is heavy-tailed (rare light paths, Russian roulette
 # weights) and each pixel's variance is estimated from its own samples, so
-# the per-pixel 3-sigma rate sits above the Gaussian 0.27%; 8x8-tile means
-# are close to Gaussian, and their rate is the one a bias would lift.
+# the per-pixel 3-sigma rate sits above the Gaussian 0.27%; tile means are
+# close to Gaussian, and their rate is the one a bias would lift. The sweep's
+# mirror-like spheres add caustic fireflies (relMSE about 0.8 at the oracle's
+# 64 spp), so its tiles are 16x16: enough samples per tile that the tile's
+# variance estimate sees the fireflies.
 def test_cornell_at_its_stated_size_unbiased_against_fp64(cuda_dev):
     """The Cornell box at 512x512, depth 8: 4,096 spp on the GPU against the
     FP64 oracle at 256 spp over the whole frame."""
@@ -106,7 +109,7 @@ def test_cornell_at_its_stated_size_unbiased_against_fp64(cuda_dev):
 def test_sweep_at_1080p_unbiased_on_a_crop(cuda_dev):
     """The material sweep at 1920x1080, depth 12: 1,024 spp on the GPU, the
     FP64 oracle at 64 spp on the 48 rows through the middle of the frame."""
-    frac, tfrac, dmean, se, rel_mse = _full_size("spheres", 1920, 1080, 12, 1024, 64, 48)
+    frac, tfrac, dmean, se, rel_mse = _full_size("spheres", 1920, 1080, 12, 1024, 64, 48, tile=16)
     assert frac < 0.025, frac
     assert tfrac < 0.01, tfrac
     assert dmean < 4 * se, (dmean, se)

@@ -63,3 +63,30 @@ def test_tail_kernel_in_batched_views(cuda_dev):
         r.close()
     for (s0, q0, n0), (s1, q1, n1) in zip(*out):
         assert n0 == n1 and np.array_equal(s0, s1) and np.array_equal(q0, q1)
+
+
+def test_tail_kernel_past_the_guided_bounces(cuda_dev):
+    """With guiding on, the path-completion kernel takes over only past the
+    guided bounces (from the guiding maxDepth + 2 on: bounce maxDepth + 1
+    still completes a training path's last record). Guided shading beyond
+    maxDepth samples the BSDF only, so online-trained guided renders are
+    the same with and without the tail kernel; a tail bounce inside the
+    guided range is ignored."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    outs = []
+    for tail in (-1, 5, 3):
+        r = opt.Renderer(sc, spp_batch=4, tail_bounce=tail)
+        r.setupOutputBuffer(64, 64)
+        r.set_guiding(1)
+        r.guiding_options(maxDepth=3)
+        r.render(16, torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        outs.append(r.accum())
+        assert r.guide().status()[0] == 0
+        r.close()
+    for s, q, n in outs[1:]:
+        assert n == outs[0][2] and np.array_equal(s, outs[0][0]) and np.array_equal(q, outs[0][1])
+    assert outs[0][0].sum() > 0
