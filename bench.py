@@ -62,8 +62,10 @@ GUIDED = {"workload": "indirect-lit interior (doorway only), 1,947,146 tris, dep
           # guided: online training for the first 1,024 samples per pixel
           # (one path in two records; 512 passes of 2 spp, each with 4 Adam
           # steps), then the network is frozen; mixture selection probability
-          # capped at 0.6
-          "guiding_options": {"trainSpp": 1024, "trainStride": 2, "alphaMax": 0.6}}
+          # capped at 0.6; the first 6 bounces guided, the path-completion
+          # kernel from bounce 8 on (plain: from bounce 5, the default)
+          "guiding_options": {"trainSpp": 1024, "trainStride": 2, "alphaMax": 0.6, "maxDepth": 6},
+          "guided_tail_bounce": 8}
 BATCH = {"workload": "batched multi-view: 96 views (48 of the terrain, 48 of the material sweep), sides "
                      "log-uniform 128..1024, spp U{16..256}, depth 12, guiding on; one batch per scene, each "
                      "autotuned with guiding on (leaf size, block size, compaction)", "views_per_scene": 48,
@@ -455,7 +457,7 @@ def guided_equal_time(stream, budget_s=None, reference_spp=None):
     w, h = g["width"], g["height"]
 
     def make(seed, mode):
-        r = opt.Renderer(scene)
+        r = opt.Renderer(scene, tail_bounce=g["guided_tail_bounce"] if mode else 0)
         r.setupOutputBuffer(w, h)
         r.set_seed(seed)
         if mode:

@@ -68,25 +68,33 @@ def test_tail_kernel_in_batched_views(cuda_dev):
 def test_tail_kernel_past_the_guided_bounces(cuda_dev):
     """With guiding on, the path-completion kernel takes over only past the
     guided bounces (from the guiding maxDepth + 2 on: bounce maxDepth + 1
-    still completes a training path's last record). Guided shading beyond
-    maxDepth samples the BSDF only, so online-trained guided renders are
-    the same with and without the tail kernel; a tail bounce inside the
-    guided range is ignored."""
+    still completes a training path's last record); a tail bounce inside the
+    guided range is ignored (the pass is the same, bit for bit). Past the
+    guided bounces both sample the BSDF only, but in differently compiled
+    code (the guided shading kernel's plain branch, the path-completion
+    kernel's plain shading), so the network trains on samples that differ in
+    rounding and the two online-trained renders are compared statistically:
+    per-pixel z scores of the difference and the frame mean."""
     import torch
 
     import optix_pt_gb300 as opt
+    from gpu_util import pixel_stats
     sc = opt.Scene.procedural("cornell")
     outs = []
-    for tail in (-1, 5, 3):
-        r = opt.Renderer(sc, spp_batch=4, tail_bounce=tail)
-        r.setupOutputBuffer(64, 64)
+    for tail in (-1, 3, 5):
+        r = opt.Renderer(sc, spp_batch=16, tail_bounce=tail)
+        r.setupOutputBuffer(48, 48)
         r.set_guiding(1)
         r.guiding_options(maxDepth=3)
-        r.render(16, torch.cuda.current_stream())
+        r.render(512, torch.cuda.current_stream())
         torch.cuda.synchronize()
-        outs.append(r.accum())
+        s, q, n = r.accum()
+        outs.append((s.reshape(-1, 3), q.reshape(-1, 3), n))
         assert r.guide().status()[0] == 0
         r.close()
-    for s, q, n in outs[1:]:
-        assert n == outs[0][2] and np.array_equal(s, outs[0][0]) and np.array_equal(q, outs[0][1])
+    assert np.array_equal(outs[1][0], outs[0][0]) and np.array_equal(outs[1][1], outs[0][1])
+    frac, dmean, se, *_ = pixel_stats(outs[2], outs[0])
+    print("guided, tail kernel from bounce 5 vs none: z>3 fraction %.4f, mean diff %.3g (SE %.3g)" % (frac, dmean, se))
+    assert frac < 0.01, frac
+    assert dmean < 4 * se, (dmean, se)
     assert outs[0][0].sum() > 0
