@@ -94,9 +94,11 @@ def _full_size(name, w, h, depth, spp_gpu, spp_cpu, rows, tile=8):
 # weights) and each pixel's variance is estimated from its own samples, so
 # the per-pixel 3-sigma rate sits above the Gaussian 0.27%; tile means are
 # close to Gaussian, and their rate is the one a bias would lift. The sweep's
-# mirror-like spheres add caustic fireflies (relMSE about 0.8 at the oracle's
-# 64 spp), so its tiles are 16x16: enough samples per tile that the tile's
-# variance estimate sees the fireflies.
+# mirror-like spheres add caustic fireflies, which a 64-spp oracle render
+# misses in many tiles, so its variance estimates run low there (measured on
+# GB300: tile rate 1.2% against 64 spp, 0.28-0.58% against 256 spp, 0.23-
+# 0.37% for the oracle's own FP32 render against its FP64 one): the sweep's
+# oracle renders 256 spp, on 32 rows.
 def test_cornell_at_its_stated_size_unbiased_against_fp64(cuda_dev):
     """The Cornell box at 512x512, depth 8: 4,096 spp on the GPU against the
     FP64 oracle at 256 spp over the whole frame."""
@@ -108,9 +110,9 @@ def test_cornell_at_its_stated_size_unbiased_against_fp64(cuda_dev):
 
 def test_sweep_at_1080p_unbiased_on_a_crop(cuda_dev):
     """The material sweep at 1920x1080, depth 12: 1,024 spp on the GPU, the
-    FP64 oracle at 64 spp on the 48 rows through the middle of the frame."""
-    frac, tfrac, dmean, se, rel_mse = _full_size("spheres", 1920, 1080, 12, 1024, 64, 48, tile=16)
-    assert frac < 0.025, frac
+    FP64 oracle at 256 spp on the 32 rows through the middle of the frame."""
+    frac, tfrac, dmean, se, rel_mse = _full_size("spheres", 1920, 1080, 12, 1024, 256, 32)
+    assert frac < 0.02, frac
     assert tfrac < 0.01, tfrac
     assert dmean < 4 * se, (dmean, se)
 

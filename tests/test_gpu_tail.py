@@ -69,12 +69,11 @@ def test_tail_kernel_past_the_guided_bounces(cuda_dev):
     """With guiding on, the path-completion kernel takes over only past the
     guided bounces (from the guiding maxDepth + 2 on: bounce maxDepth + 1
     still completes a training path's last record); a tail bounce inside the
-    guided range is ignored (the pass is the same, bit for bit). Past the
-    guided bounces both sample the BSDF only, but in differently compiled
-    code (the guided shading kernel's plain branch, the path-completion
-    kernel's plain shading), so the network trains on samples that differ in
-    rounding and the two online-trained renders are compared statistically:
-    per-pixel z scores of the difference and the frame mean."""
+    guided range is ignored. Online training adds hash-grid gradients with
+    atomics, in no fixed order, so two guided renders differ in rounding even
+    with the same settings; the renders are therefore compared statistically
+    (per-pixel z scores of the difference and the frame mean) with the
+    render that has no tail kernel."""
     import torch
 
     import optix_pt_gb300 as opt
@@ -92,9 +91,9 @@ def test_tail_kernel_past_the_guided_bounces(cuda_dev):
         outs.append((s.reshape(-1, 3), q.reshape(-1, 3), n))
         assert r.guide().status()[0] == 0
         r.close()
-    assert np.array_equal(outs[1][0], outs[0][0]) and np.array_equal(outs[1][1], outs[0][1])
-    frac, dmean, se, *_ = pixel_stats(outs[2], outs[0])
-    print("guided, tail kernel from bounce 5 vs none: z>3 fraction %.4f, mean diff %.3g (SE %.3g)" % (frac, dmean, se))
-    assert frac < 0.01, frac
-    assert dmean < 4 * se, (dmean, se)
+    for k, tail in ((1, 3), (2, 5)):
+        frac, dmean, se, *_ = pixel_stats(outs[k], outs[0])
+        print("guided, tail bounce %d vs none: z>3 fraction %.4f, mean diff %.3g (SE %.3g)" % (tail, frac, dmean, se))
+        assert frac < 0.01, (tail, frac)
+        assert dmean < 4 * se, (tail, dmean, se)
     assert outs[0][0].sum() > 0
