@@ -522,7 +522,8 @@ typedef struct optpt_view {
     uint32_t width;
     uint32_t height;
     uint32_t spp;
-    uint32_t pad;
+    uint32_t scene;  /* optpt_render_batch_scenes: index of the view's renderer
+                      * (its scene); ignored by optpt_render_batch */
 } optpt_view;
 
 /* Renders every view to its spp in shared wavefront passes (the reference
@@ -535,6 +536,19 @@ typedef struct optpt_view {
  * (view 0 therefore matches a single-view render bit for bit). Guiding, if
  * on, guides and trains on every view. Accumulators restart at each call. */
 int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numViews, void *stream);
+
+/* Views of several scenes in one batch: renderers[k] holds scene k (its own
+ * BVH, materials, lights and guiding network) and view.scene picks the
+ * renderer of each view. Every pass is ONE CUDA graph launch whose child
+ * graphs are the scenes' captured batch passes, with no dependency between
+ * them, so the scenes' bounce loops run side by side on the GPU (a scene
+ * whose views are done drops out of the launch). Each renderer's batch holds
+ * its own views in the order given: after the call, optpt_batch_view(
+ * renderers[k], j, ...) is the j-th view of scene k, bit-identical to the
+ * same views rendered by optpt_render_batch on that renderer alone. No
+ * counterpart in the reference (one view of one scene per launch). */
+int optpt_render_batch_scenes(optpt_renderer *const *renderers, uint32_t numScenes, const optpt_view *views,
+                              uint32_t numViews, void *stream);
 
 /* Device pointers into the last batch's buffers for one view: FP64 sums and
  * sums of squares (double4 per pixel, xyz used), the tone-mapped float4

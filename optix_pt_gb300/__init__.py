@@ -16,7 +16,7 @@ from . import _ffi
 from ._ffi import BSDF_QUERY, BSDF_RESULT, OptptError, check, lib
 
 __all__ = ["Scene", "SceneDesc", "GltfModel", "Animator", "decode_png", "decode_jpeg", "encode_png", "encode_hdr", "encode_exr", "Renderer", "OptptError", "bsdf_batch", "BSDF_QUERY", "BSDF_RESULT",
-           "library_path"]
+           "library_path", "render_batch_scenes", "autotune"]
 
 library_path = _ffi.LIB_PATH
 
@@ -644,6 +644,25 @@ class Guide:
         n = ctypes.c_double()
         check(lib.optpt_guide_status(self._h, ctypes.byref(st), ctypes.byref(loss), ctypes.byref(n)))
         return st.value, loss.value, n.value
+
+
+def render_batch_scenes(renderers, views, stream=None):
+    """Views of several scenes in one batch (optpt_render_batch_scenes):
+    views = [(scene index, (eye, target, up, fovYDeg, width, height, spp)),
+    ...]; renderers[k] renders scene k. Every pass is one graph launch over
+    all scenes. Afterwards renderers[k].batch_view(j) is the j-th view of
+    scene k; returns, per view in the order given, (k, j)."""
+    arr = (_ffi.View * len(views))()
+    where, count = [], [0] * len(renderers)
+    for i, (k, (eye, target, up, fov, w, h, spp)) in enumerate(views):
+        arr[i] = _ffi.View(_ffi.f3(*eye), _ffi.f3(*target), _ffi.f3(*up), fov, w, h, spp, k)
+        where.append((k, count[k]))
+        count[k] += 1
+    hs = (ctypes.c_void_p * len(renderers))(*[r._h.value for r in renderers])
+    check(lib.optpt_render_batch_scenes(hs, len(renderers), arr, len(views), _stream_handle(stream)))
+    for k, r in enumerate(renderers):
+        r._batch_shapes = [(v[4], v[5]) for kk, v in views if kk == k]
+    return where
 
 
 def autotune(scene, width, height, spp, warmup_spp=2, guiding=0):

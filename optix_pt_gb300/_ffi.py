@@ -147,7 +147,7 @@ class AutotuneTrial(ctypes.Structure):
 
 class View(ctypes.Structure):
     _fields_ = [("eye", f3), ("target", f3), ("up", f3), ("fovYDeg", ctypes.c_float), ("width", ctypes.c_uint32),
-                ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+                ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32), ("scene", ctypes.c_uint32)]
 
 
 class TraversalCounts(ctypes.Structure):
@@ -245,6 +245,8 @@ _sigs = {
     "optpt_queue_counts": (ctypes.c_int, [_H, _P, _P, _P, ctypes.c_uint32]),
     "optpt_guiding_batch": (ctypes.c_int, [_H, _P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
     "optpt_render_batch": (ctypes.c_int, [_H, ctypes.POINTER(View), ctypes.c_uint32, _P]),
+    "optpt_render_batch_scenes": (ctypes.c_int, [ctypes.POINTER(_H), ctypes.c_uint32, ctypes.POINTER(View),
+                                                 ctypes.c_uint32, _P]),
     "optpt_autotune": (ctypes.c_int, [ctypes.POINTER(SceneStruct), ctypes.POINTER(AutotuneRequest),
                                       ctypes.POINTER(Options), ctypes.POINTER(AutotuneTrial), ctypes.c_uint32,
                                       ctypes.POINTER(ctypes.c_uint32)]),

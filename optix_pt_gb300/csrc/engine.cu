@@ -137,6 +137,12 @@ struct optpt_renderer {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         int guideMode = -1;
+        // per-pass host state (batchPassSizes)
+        std::vector<char> wasActive;
+        std::vector<uint32_t> list;
+        std::vector<BatchView> hostViews;
+        uint32_t per = 0;
+        uint32_t dyn[2] = {0, 0};
     } batch;
 
     void freeBatch()
@@ -903,7 +909,14 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
     return OPTPT_OK;
 }
 
-int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numViews, void *stream)
+}  // extern "C"
+
+namespace {
+
+// Batched multi-view rendering, step 1: checks the views, (re)allocates the
+// batch buffers for their pixel layout, restarts the accumulators and
+// captures the batch pass (once per layout and guiding mode).
+int batchSetup(optpt_renderer *r, const optpt_view *views, uint32_t numViews, cudaStream_t st)
 {
     if (!r || (numViews && !views))
         return fail(OPTPT_ERR_INVALID, "NULL argument");
@@ -918,7 +931,6 @@ int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numV
     }
     if (total > (1u << 30))
         return fail(OPTPT_ERR_INVALID, "more than 2^30 pixels in one batch");
-    cudaStream_t st = (cudaStream_t)stream;
     auto &B = r->batch;
     if (r->shape.block == 0) {
         const int blk = r->opt.blockSize ? (int)r->opt.blockSize : 128;
@@ -1016,58 +1028,181 @@ int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numV
         CUDA_OR_RETURN(cudaGraphInstantiate(&B.exec, B.graph, 0), "batch instantiate");
         B.guideMode = r->guideMode;
     }
-    std::vector<BatchView> hv(numViews);
-    std::vector<uint32_t> list;
-    std::vector<char> wasActive(numViews, 0);
-    for (;;) {
-        uint32_t active = 0, minLeft = UINT32_MAX;
-        bool changed = false;
-        for (uint32_t v = 0; v < numViews; ++v) {
-            const bool a = B.done[v] < views[v].spp;
-            changed |= (a != (bool)wasActive[v]);
-            wasActive[v] = a;
-            if (a) {
-                active += views[v].width * views[v].height;
-                minLeft = std::min(minLeft, views[v].spp - B.done[v]);
-            }
+    B.wasActive.assign(numViews, 0);
+    B.list.clear();
+    B.per = 0;
+    return OPTPT_OK;
+}
+
+// Step 2, once per pass: picks the views that still need samples and the
+// samples per pixel of this pass, and uploads the active-pixel list (when it
+// changed), the view table and the pass sizes on `st`. *more = false when
+// every view is done (nothing is uploaded then).
+int batchPassSizes(optpt_renderer *r, cudaStream_t st, bool *more)
+{
+    auto &B = r->batch;
+    const std::vector<optpt_view> &views = B.views;
+    const uint32_t numViews = (uint32_t)views.size();
+    uint32_t active = 0, minLeft = UINT32_MAX;
+    bool changed = false;
+    for (uint32_t v = 0; v < numViews; ++v) {
+        const bool a = B.done[v] < views[v].spp;
+        changed |= (a != (bool)B.wasActive[v]);
+        B.wasActive[v] = a;
+        if (a) {
+            active += views[v].width * views[v].height;
+            minLeft = std::min(minLeft, views[v].spp - B.done[v]);
         }
-        if (active == 0)
-            break;
-        if (changed) {
-            list.clear();
-            for (uint32_t v = 0; v < numViews; ++v)
-                if (wasActive[v])
-                    for (uint32_t k = 0; k < views[v].width * views[v].height; ++k)
-                        list.push_back(B.first[v] + k);
-            CUDA_OR_RETURN(cudaMemcpyAsync(B.dPixelList, list.data(), sizeof(uint32_t) * list.size(),
-                                           cudaMemcpyHostToDevice, st),
-                           "batch list");
-        }
-        const uint32_t per = std::max(1u, std::min(minLeft, B.maxPaths / active));
-        for (uint32_t v = 0; v < numViews; ++v) {
-            const optpt_view &V = views[v];
-            float U[3], Vv[3], W[3];
-            cameraBasis(V.eye, V.target, V.up, V.fovYDeg, (float)V.width / (float)V.height, U, Vv, W);
-            auto bits = [](uint32_t u) {
-                float f;
-                memcpy(&f, &u, 4);
-                return f;
-            };
-            hv[v].eye = make_float4(V.eye[0], V.eye[1], V.eye[2], bits(V.width));
-            hv[v].U = make_float4(U[0], U[1], U[2], bits(V.height));
-            hv[v].V = make_float4(Vv[0], Vv[1], Vv[2], bits(B.first[v]));
-            hv[v].W = make_float4(W[0], W[1], W[2], bits(B.done[v]));
-        }
-        const uint32_t dyn[2] = {active, per};
-        CUDA_OR_RETURN(cudaMemcpyAsync(B.dViews, hv.data(), sizeof(BatchView) * numViews, cudaMemcpyHostToDevice, st),
-                       "batch views");
-        CUDA_OR_RETURN(cudaMemcpyAsync(B.dDyn, dyn, sizeof(dyn), cudaMemcpyHostToDevice, st), "batch sizes");
-        CUDA_OR_RETURN(cudaGraphLaunch(B.exec, st), "batch launch");
+    }
+    *more = active != 0;
+    if (!*more)
+        return OPTPT_OK;
+    if (changed) {
+        B.list.clear();
         for (uint32_t v = 0; v < numViews; ++v)
-            if (wasActive[v])
-                B.done[v] += per;
+            if (B.wasActive[v])
+                for (uint32_t k = 0; k < views[v].width * views[v].height; ++k)
+                    B.list.push_back(B.first[v] + k);
+        CUDA_OR_RETURN(cudaMemcpyAsync(B.dPixelList, B.list.data(), sizeof(uint32_t) * B.list.size(),
+                                       cudaMemcpyHostToDevice, st),
+                       "batch list");
+    }
+    B.per = std::max(1u, std::min(minLeft, B.maxPaths / active));
+    B.hostViews.resize(numViews);
+    for (uint32_t v = 0; v < numViews; ++v) {
+        const optpt_view &V = views[v];
+        float U[3], Vv[3], W[3];
+        cameraBasis(V.eye, V.target, V.up, V.fovYDeg, (float)V.width / (float)V.height, U, Vv, W);
+        auto bits = [](uint32_t u) {
+            float f;
+            memcpy(&f, &u, 4);
+            return f;
+        };
+        B.hostViews[v].eye = make_float4(V.eye[0], V.eye[1], V.eye[2], bits(V.width));
+        B.hostViews[v].U = make_float4(U[0], U[1], U[2], bits(V.height));
+        B.hostViews[v].V = make_float4(Vv[0], Vv[1], Vv[2], bits(B.first[v]));
+        B.hostViews[v].W = make_float4(W[0], W[1], W[2], bits(B.done[v]));
+    }
+    B.dyn[0] = active;
+    B.dyn[1] = B.per;
+    CUDA_OR_RETURN(cudaMemcpyAsync(B.dViews, B.hostViews.data(), sizeof(BatchView) * numViews,
+                                   cudaMemcpyHostToDevice, st),
+                   "batch views");
+    CUDA_OR_RETURN(cudaMemcpyAsync(B.dDyn, B.dyn, sizeof(B.dyn), cudaMemcpyHostToDevice, st), "batch sizes");
+    return OPTPT_OK;
+}
+
+// Step 3, after the pass is enqueued: the active views' sample counts.
+void batchPassDone(optpt_renderer *r)
+{
+    auto &B = r->batch;
+    for (size_t v = 0; v < B.views.size(); ++v)
+        if (B.wasActive[v])
+            B.done[v] += B.per;
+}
+
+}  // namespace
+
+extern "C" {
+
+int optpt_render_batch(optpt_renderer *r, const optpt_view *views, uint32_t numViews, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = batchSetup(r, views, numViews, st);
+    if (rc)
+        return rc;
+    for (;;) {
+        bool more = false;
+        if ((rc = batchPassSizes(r, st, &more)))
+            return rc;
+        if (!more)
+            break;
+        CUDA_OR_RETURN(cudaGraphLaunch(r->batch.exec, st), "batch launch");
+        batchPassDone(r);
     }
     CUDA_OR_RETURN(cudaGetLastError(), "batch");
+    return OPTPT_OK;
+}
+
+int optpt_render_batch_scenes(optpt_renderer *const *renderers, uint32_t numScenes, const optpt_view *views,
+                              uint32_t numViews, void *stream)
+{
+    if (!renderers || numScenes == 0 || numScenes > 32 || !views || numViews == 0)
+        return fail(OPTPT_ERR_INVALID, "1 to 32 renderers and at least one view");
+    for (uint32_t k = 0; k < numScenes; ++k)
+        if (!renderers[k])
+            return fail(OPTPT_ERR_INVALID, "NULL renderer");
+    std::vector<std::vector<optpt_view>> per(numScenes);
+    for (uint32_t v = 0; v < numViews; ++v) {
+        if (views[v].scene >= numScenes)
+            return fail(OPTPT_ERR_INVALID, "view " + std::to_string(v) + ": scene index out of range");
+        per[views[v].scene].push_back(views[v]);
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc;
+    for (uint32_t k = 0; k < numScenes; ++k)
+        if (!per[k].empty() && (rc = batchSetup(renderers[k], per[k].data(), (uint32_t)per[k].size(), st)))
+            return rc;
+    // One graph per set of still-active scenes: each scene's captured batch
+    // pass is a child graph, with no dependency between them, so one launch
+    // runs every scene's pass and their bounce loops proceed side by side.
+    std::vector<std::pair<uint32_t, cudaGraphExec_t>> execs;
+    std::vector<cudaGraph_t> graphs;
+    auto cleanup = [&]() {
+        for (auto &e : execs)
+            cudaGraphExecDestroy(e.second);
+        for (cudaGraph_t g : graphs)
+            cudaGraphDestroy(g);
+    };
+    for (;;) {
+        uint32_t mask = 0;
+        for (uint32_t k = 0; k < numScenes; ++k) {
+            if (per[k].empty())
+                continue;
+            bool more = false;
+            if ((rc = batchPassSizes(renderers[k], st, &more))) {
+                cleanup();
+                return rc;
+            }
+            if (more)
+                mask |= 1u << k;
+        }
+        if (mask == 0)
+            break;
+        cudaGraphExec_t exec = nullptr;
+        for (auto &e : execs)
+            if (e.first == mask)
+                exec = e.second;
+        if (!exec) {
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaGraphCreate(&g, 0);
+            for (uint32_t k = 0; e == cudaSuccess && k < numScenes; ++k) {
+                cudaGraphNode_t node;
+                if (mask & (1u << k))
+                    e = cudaGraphAddChildGraphNode(&node, g, nullptr, 0, renderers[k]->batch.graph);
+            }
+            if (e == cudaSuccess)
+                e = cudaGraphInstantiate(&exec, g, 0);
+            if (g)
+                graphs.push_back(g);
+            if (e != cudaSuccess) {
+                cleanup();
+                return cudaFail(e, "multi-scene batch graph");
+            }
+            execs.emplace_back(mask, exec);
+        }
+        cudaError_t e = cudaGraphLaunch(exec, st);
+        if (e != cudaSuccess) {
+            cleanup();
+            return cudaFail(e, "multi-scene batch launch");
+        }
+        for (uint32_t k = 0; k < numScenes; ++k)
+            if (mask & (1u << k))
+                batchPassDone(renderers[k]);
+    }
+    // the graphs may be destroyed once their launches are enqueued
+    cleanup();
+    CUDA_OR_RETURN(cudaGetLastError(), "multi-scene batch");
     return OPTPT_OK;
 }
 
