@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(256, OPTPT_TRAV_MINB)
 // ray totals and per-bounce counts stay exact. Plain sampling only (guided
 // shading needs the batched inference between extension and shading).
 template <bool COUNT, bool WIDE>
-__global__ void __launch_bounds__(128) kFinish(DevScene s, FrameParams fp, WaveBufs q, int depth0)
+__global__ void __launch_bounds__(128, 4) kFinish(DevScene s, FrameParams fp, WaveBufs q, int depth0)
 {
     const uint32_t count = q.counters[CNT_EXT + depth0];
     const int cur = depth0 & 1;
