@@ -297,6 +297,10 @@ def roofline_of(name, r, prof, cnt, w, h, bvh_width, sm_mhz):
             "issue_bound": issue}
 
 
+def _launches_per_pass(max_depth, tail):
+    return 3 + (4 * (tail - 1) + 1 if tail else 4 * max_depth)
+
+
 def measure_frames(name, args, rank, world, dev, stream, with_cpu):
     """One workload of 1-spp passes: device-timed throughput (L2 flushed
     between steps), end-to-end throughput through the public API with host
@@ -382,7 +386,9 @@ def measure_frames(name, args, rank, world, dev, stream, with_cpu):
     out = {"value": value, "ms_per_step": ms_all / args.steps, "samples_per_s": samples_all / (ms_all / 1e3),
            "rays_per_step": rays_all / args.steps / world,
            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": 80, "d2h_bytes_per_step": w * h * 16},
-           "gpu_launches": (3 + 4 * wl["max_depth"]) * args.steps}
+           # per pass: generate, accumulate, advance, 4 per bounce (extend,
+           # shade, 2 shadow) up to the path-completion bounce, then 1
+           "gpu_launches": _launches_per_pass(wl["max_depth"], r.stats()["tailBounce"]) * args.steps}
     if rank == 0:
         prof = r.profile(2, stream)
         cnt = r.traversal_counts(1, stream)

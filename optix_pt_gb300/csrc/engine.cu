@@ -1129,9 +1129,13 @@ int optpt_render_batch_scenes(optpt_renderer *const *renderers, uint32_t numScen
 {
     if (!renderers || numScenes == 0 || numScenes > 32 || !views || numViews == 0)
         return fail(OPTPT_ERR_INVALID, "1 to 32 renderers and at least one view");
-    for (uint32_t k = 0; k < numScenes; ++k)
+    for (uint32_t k = 0; k < numScenes; ++k) {
         if (!renderers[k])
             return fail(OPTPT_ERR_INVALID, "NULL renderer");
+        for (uint32_t j = 0; j < k; ++j)
+            if (renderers[j] == renderers[k])
+                return fail(OPTPT_ERR_INVALID, "a renderer appears twice (one renderer per scene)");
+    }
     std::vector<std::vector<optpt_view>> per(numScenes);
     for (uint32_t v = 0; v < numViews; ++v) {
         if (views[v].scene >= numScenes)
