@@ -206,9 +206,10 @@ typedef struct optpt_options {
                           * remaining path (closest hit, shading and shadow rays
                           * per bounce, bit-identical to the per-bounce kernels)
                           * instead of a launch per kernel per bounce; with
-                          * guiding on only if it is past the guided bounces
-                          * (>= guiding maxDepth + 2); 0 =
-                          * OPTPT_DEFAULT_TAIL_BOUNCE, 0xFFFFFFFF = never       */
+                          * guiding on it starts past the guided bounces, at
+                          * guiding maxDepth + 1 at the earliest (+ 2 while the
+                          * network trains); 0 = OPTPT_DEFAULT_TAIL_BOUNCE,
+                          * 0xFFFFFFFF = never                                  */
 } optpt_options;
 #define OPTPT_DEFAULT_TAIL_BOUNCE 5
 
@@ -463,6 +464,16 @@ int optpt_guide_levels(optpt_guide *g, float *res, uint32_t *dense, float *lo, f
  * each, as halves: per lobe (mu.xyz, kappa), then the 8 weights, then the
  * probability of sampling the mixture rather than the BSDF, then 7 zeros. */
 int optpt_guide_infer(optpt_guide *g, const float *queries, uint32_t n, void *mixtures, void *stream);
+
+/* The renderer's own mixture sampler and density (the device functions its
+ * shading kernel calls) on n packed mixtures, device arrays in the layout
+ * optpt_guide_infer writes. With xi (3 floats per mixture in [0, 1)) each
+ * row draws a direction as a guided vertex does (the lobe by xi[0], the
+ * direction from it by 1 - xi[1] and xi[2]) and dirPdf (4 floats per row)
+ * receives (direction, mixture density there); with xi NULL, dirPdf holds a
+ * unit direction per row on input and its 4th float receives the density.
+ * Asynchronous on `stream`. */
+int optpt_guide_mixture_eval(const void *mixtures, uint32_t n, const float *xi, float *dirPdf, void *stream);
 
 /* Gradient of the batch loss: for the selection probability a (a learned
  * output), sum_i -c_i log(a q(wi_i) + (1 - a) pb_i), the density of the

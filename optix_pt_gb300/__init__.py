@@ -626,6 +626,13 @@ class Guide:
     def infer(self, queries_ptr, n, mixtures_ptr, stream=None):
         check(lib.optpt_guide_infer(self._h, queries_ptr, n, mixtures_ptr, _stream_handle(stream)))
 
+    @staticmethod
+    def mixture_eval(mixtures_ptr, n, xi_ptr, dir_pdf_ptr, stream=None):
+        """The renderer's mixture sampler and density (device pointers):
+        with xi_ptr, rows of (direction, density) drawn as a guided vertex
+        draws them; with xi_ptr None, densities at the given directions."""
+        check(lib.optpt_guide_mixture_eval(mixtures_ptr, n, xi_ptr, dir_pdf_ptr, _stream_handle(stream)))
+
     def gradients(self, samples_ptr, count_ptr, capacity, stream=None):
         dm = np.zeros(self.MLP_PARAMS, np.float32)
         dh = np.zeros(self.HASH_PARAMS, np.float32)

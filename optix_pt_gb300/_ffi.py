@@ -235,6 +235,7 @@ _sigs = {
     "optpt_guide_params": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     "optpt_guide_levels": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "optpt_guide_infer": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P, _P]),
+    "optpt_guide_mixture_eval": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P, _P]),
     "optpt_guide_gradients": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P, _P, ctypes.POINTER(ctypes.c_double),
                                              _P]),
     "optpt_guide_train_step": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P]),

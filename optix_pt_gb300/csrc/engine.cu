@@ -423,14 +423,15 @@ int enqueuePassOn(optpt_renderer *r, const FrameParams &fp, const WaveBufs &q, c
     launchGenerate(r->shape, fp, q, st);
     // From bounce tailBounce on, one launch finishes every remaining path
     // (launchFinish) instead of a launch per kernel per bounce. It samples
-    // the BSDF only, so with guiding on it takes over only past the guided
-    // bounces: from guide.maxDepth + 2 on, since the guided shading of bounce
-    // guide.maxDepth + 1 still writes the arrival record of a training path's
-    // last guided vertex.
-    const uint32_t tail = !fp.guide.on ? r->tailBounce
-                          : (fp.guide.maxDepth < OPT_MAX_DEPTH && r->tailBounce >= fp.guide.maxDepth + 2u
-                                 ? r->tailBounce
-                                 : 0u);
+    // the BSDF only, so with guiding on it starts past the guided bounces:
+    // at guide.maxDepth + 1 at the earliest, and at guide.maxDepth + 2 while
+    // the network trains, since the shading of bounce guide.maxDepth + 1 then
+    // writes the arrival record of a training path's last guided vertex.
+    uint32_t tail = r->tailBounce;
+    if (fp.guide.on && tail != 0u)
+        tail = fp.guide.maxDepth < OPT_MAX_DEPTH
+                   ? std::max(tail, fp.guide.maxDepth + (fp.guide.train ? 2u : 1u))
+                   : 0u;
     for (uint32_t d = 1; d <= fp.maxDepth; ++d) {
         if (d == tail) {
             if (fork && d > 1)

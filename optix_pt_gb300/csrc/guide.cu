@@ -16,9 +16,11 @@
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 #include "optpt.h"
 #include "tc.cuh"
@@ -72,7 +74,8 @@ __device__ __forceinline__ float3 unitPos(const GuideGeom &g, float3 p)
                fminf(fmaxf((p.z - g.lo.z) * g.invExt.z, 0.0f), one));
 }
 
-// Input row: hash features (FP32 table for training, FP16 copy for inference).
+// Input row: hash features (FP32 table for training; for inference the FP16
+// pair copy, whose slot e holds entry e's features followed by entry e + 1's).
 // Each level's two features go straight to shared memory (one 32-bit store),
 // so the level loop stays rolled: a fully unrolled 16 x 8 gather loop costs
 // more in instruction fetch than it saves.
@@ -82,32 +85,47 @@ __device__ void encodeRow(const GuideGeom &g, const float *hash, const __half *h
 {
     if (valid) {
         const float3 p = unitPos(g, pos);
-        // four levels at a time: their 32 gathers are issued before any is used
+        // four levels at a time: their 32 gathers are issued before any is
+        // used; only the raw features and each level's fractions live across
+        // the gathers (the corner weights are formed as they are consumed)
+        using Raw = typename std::conditional<HALF, __half2, float2>::type;
 #pragma unroll 1
         for (int l0 = 0; l0 < LEVELS; l0 += 4) {
-            uint32_t e[4][8];
-            float w[4][8];
+            float t[4][3];
+            Raw v[4][8];
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                levelCorners(g.levels, l0 + j, p.x, p.y, p.z, e[j], w[j]);
-            float2 v[4][8];
+            for (int j = 0; j < 4; ++j) {
+                uint32_t e[8];
+                levelCell(g.levels, l0 + j, p.x, p.y, p.z, e, t[j][0], t[j][1], t[j][2]);
+                if constexpr (HALF) {
+                    // pair copy: entry e's features, then entry e + 1's
+                    // (corner c + 1 is corner c's x-neighbour)
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+                    for (int c = 0; c < 8; c += 2) {
+                        const uint2 pr =
+                            __ldg(reinterpret_cast<const uint2 *>(hashH) + ((size_t)(l0 + j) * TABLE + e[c]));
+                        v[j][c] = *reinterpret_cast<const __half2 *>(&pr.x);
+                        v[j][c + 1] = *reinterpret_cast<const __half2 *>(&pr.y);
+                    }
+                } else {
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    const size_t at = ((size_t)(l0 + j) * TABLE + e[j][c]) * FEATS;
-                    if (HALF)
-                        v[j][c] = __half22float2(__ldg(reinterpret_cast<const __half2 *>(hashH + at)));
-                    else
-                        v[j][c] = __ldg(reinterpret_cast<const float2 *>(hash + at));
+                    for (int c = 0; c < 8; ++c)
+                        v[j][c] = __ldg(reinterpret_cast<const float2 *>(hash + ((size_t)(l0 + j) * TABLE + e[c]) * FEATS));
                 }
+            }
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 float f0 = 0.0f, f1 = 0.0f;
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
-                    f0 += w[j][c] * v[j][c].x;
-                    f1 += w[j][c] * v[j][c].y;
+                    const float w = cornerWeight(c, t[j][0], t[j][1], t[j][2]);
+                    float2 f;
+                    if constexpr (HALF)
+                        f = __half22float2(v[j][c]);
+                    else
+                        f = v[j][c];
+                    f0 += w * f.x;
+                    f1 += w * f.y;
                 }
                 *reinterpret_cast<__nv_bfloat162 *>(tile + tc::tileOffset(row, 2 * (l0 + j))) =
                     __floats2bfloat162_rn(f0, f1);
@@ -259,29 +277,41 @@ struct HitInput {
     }
 };
 
-constexpr uint32_t INFER_SMEM = LAYERS * W_BYTES + 2 * TILE_BYTES + 1024;
+// Inference CTA shape: INFER_GROUPS groups of 128 threads, each with its own
+// 128-row activation tile, mbarrier, 64 TMEM columns and named barrier, all
+// sharing one copy of the weights; INFER_MINB CTAs resident per SM. While
+// one group waits on its MMA the others gather or convert.
+#ifndef OPTPT_INFER_GROUPS
+#define OPTPT_INFER_GROUPS 2
+#endif
+#ifndef OPTPT_INFER_MINB
+#define OPTPT_INFER_MINB 2
+#endif
+constexpr int INFER_GROUPS = OPTPT_INFER_GROUPS;
+constexpr int INFER_THREADS = 128 * INFER_GROUPS;
+constexpr uint32_t INFER_SMEM = LAYERS * W_BYTES + INFER_GROUPS * TILE_BYTES + 1024;
+// TMEM columns per CTA: a power of two of at least 32
+constexpr uint32_t INFER_TMEM = INFER_GROUPS <= 2 ? 128u : INFER_GROUPS <= 4 ? 256u : 512u;
+static_assert(INFER_GROUPS >= 1 && INFER_GROUPS <= 8, "inference groups");
+static_assert(INFER_TMEM * OPTPT_INFER_MINB <= 512, "TMEM columns of the resident CTAs");
 
-// Two 128-row tiles in flight per CTA: threads 0-127 and 128-255 are two
-// groups with their own activation tile, mbarrier, TMEM columns and named
-// barrier, sharing one copy of the weights; while one group waits on its MMA
-// the other gathers or converts.
 template <class In>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(INFER_THREADS, OPTPT_INFER_MINB)
     kGuideInfer(GuideGeom g, const __half *hashH, const uint8_t *tiles, In in, Packed *out, int *status)
 {
     extern __shared__ uint8_t smRaw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smRaw) + 1023) & ~uintptr_t(1023));
     const int t = threadIdx.x, grp = t >> 7, row = t & 127;
     uint8_t *sW = sm, *sX = sm + LAYERS * W_BYTES + grp * TILE_BYTES;
-    __shared__ uint64_t barLoad, barMma[2];
+    __shared__ uint64_t barLoad, barMma[INFER_GROUPS];
     __shared__ uint32_t tmemBase;
     if (t == 0) {
         tc::mbarInit(&barLoad, 1);
-        tc::mbarInit(&barMma[0], 1);
-        tc::mbarInit(&barMma[1], 1);
+        for (int k = 0; k < INFER_GROUPS; ++k)
+            tc::mbarInit(&barMma[k], 1);
     }
     if (t < 32)
-        tc::tmemAlloc(&tmemBase, 128);
+        tc::tmemAlloc(&tmemBase, INFER_TMEM);
     tc::fenceBeforeSync();
     __syncthreads();
     tc::fenceAfterSync();
@@ -295,12 +325,13 @@ __global__ void __launch_bounds__(256, 2)
     GroupSync sync{&barMma[grp], 0, 1 + grp};
     in.resolve();
     const uint32_t n = in.count();
-    for (uint32_t base = (blockIdx.x * 2 + grp) * TILE_ROWS; ok && base < n; base += gridDim.x * 2 * TILE_ROWS) {
+    const uint32_t lane = (uint32_t)(32 * ((t >> 5) & 3)) << 16;  // the warp's TMEM lane quarter
+    for (uint32_t base = (blockIdx.x * INFER_GROUPS + grp) * TILE_ROWS; ok && base < n;
+         base += gridDim.x * INFER_GROUPS * TILE_ROWS) {
         float3 p, nrm, wo;
         const bool valid = in.fetch(base + row, p, nrm, wo);
         encodeRow<true>(g, nullptr, hashH, p, nrm, wo, valid, sX, row);
-        float v[WIDTH];
-        for (int l = 0; l < LAYERS && ok; ++l) {
+        for (int l = 0; l < LAYERS - 1 && ok; ++l) {
             sync.toTensor();
             if (row == 0) {
                 issueLayer(tm, sX, sW + l * W_BYTES);
@@ -309,21 +340,45 @@ __global__ void __launch_bounds__(256, 2)
             ok = sync.wait();
             if (!ok)
                 break;
-            loadRow(tm, 0, v);
-            if (l < LAYERS - 1) {
+            // hidden layer: ReLU, back to the activation tile in two
+            // 32-column halves (the MMA reading sX has completed)
 #pragma unroll
-                for (int c8 = 0; c8 < WIDTH; c8 += 8) {
+            for (int h = 0; h < 2; ++h) {
+                float v[32];
+                tc::ld32(tm + lane + 32u * h, v);
+#pragma unroll
+                for (int c8 = 0; c8 < 32; c8 += 8) {
                     float r[8];
 #pragma unroll
                     for (int k = 0; k < 8; ++k)
                         r[k] = fmaxf(v[c8 + k], 0.0f);
-                    storeRow8(sX, row, c8, r);  // overwrite: the MMA reading sX has completed
+                    storeRow8(sX, row, 32 * h + c8, r);
                 }
             }
         }
+        if (ok) {
+            sync.toTensor();
+            if (row == 0) {
+                issueLayer(tm, sX, sW + (LAYERS - 1) * W_BYTES);
+                tc::commit(&barMma[grp]);
+            }
+            ok = sync.wait();
+        }
+        // the 41 outputs: columns 0-31, then 32-47. tcgen05.ld is a
+        // warp-collective (.sync.aligned) instruction: every lane of the warp
+        // loads, valid row or not, and only the decoding depends on the row.
+        float o[48];
+        if (ok) {
+            float lo[32], hi[16];
+            tc::ld32(tm + lane, lo);
+            tc::ld16(tm + lane + 32u, hi);
+#pragma unroll
+            for (int k = 0; k < 48; ++k)
+                o[k] = k < 32 ? lo[k] : hi[k - 32];
+        }
         if (ok && valid) {
             Mixture m;
-            decodeOutputs(v, m);
+            decodeOutputs(o, m);
             Packed pk;
             pack(m, pk);
             out[base + row] = pk;
@@ -340,7 +395,17 @@ __global__ void __launch_bounds__(256, 2)
     __syncthreads();
     tc::fenceAfterSync();
     if (t < 32)
-        tc::tmemFree(tmemBase, 128);
+        tc::tmemFree(tmemBase, INFER_TMEM);
+}
+
+// The shading kernel's mixture sampler and density on given rows.
+__global__ void kMixtureEval(const Packed *mix, uint32_t n, const float *xi, float4 *dirPdf)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Packed p = mix[i];
+        const float3 d = xi ? mixtureSample(p, xi[3 * i], 1.0f - xi[3 * i + 1], xi[3 * i + 2]) : f3of4(dirPdf[i]);
+        dirPdf[i] = make_float4(d.x, d.y, d.z, mixturePdf(p, d));
+    }
 }
 
 // ------------------------------------------------------------------ training
@@ -650,6 +715,16 @@ __device__ __forceinline__ void biasCorrection(const uint32_t *step, float &c1, 
     c2 = 1.0f / (1.0f - powf(BETA2, t));
 }
 
+// Parameter i of the FP32 table into the FP16 pair copy: slot e holds
+// (entry e, entry e + 1) of its level, so entry e's feature f goes to slot e
+// (first half) and slot e - 1 (second half), modulo the table.
+__device__ __forceinline__ void writePair(__half *ph, size_t i, __half h)
+{
+    const size_t f = i % FEATS, e = (i / FEATS) % TABLE, l = i / ((size_t)FEATS * TABLE);
+    ph[((l * TABLE + e) * 2) * FEATS + f] = h;
+    ph[((l * TABLE + ((e + TABLE - 1) & (TABLE - 1))) * 2 + 1) * FEATS + f] = h;
+}
+
 __global__ void kAdamHash(float *p, __half *ph, float *gr, float *m, float *v, size_t n, float lr, const uint32_t *step)
 {
     float c1, c2;
@@ -663,7 +738,7 @@ __global__ void kAdamHash(float *p, __half *ph, float *gr, float *m, float *v, s
         vi = BETA2 * vi + (1.0f - BETA2) * g * g;
         const float x = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + ADAM_EPS);
         p[i] = x;
-        ph[i] = __float2half_rn(x);
+        writePair(ph, i, __float2half_rn(x));
         m[i] = mi;
         v[i] = vi;
         gr[i] = 0.0f;
@@ -704,7 +779,7 @@ __global__ void kBuildTiles(const float *p, uint8_t *tiles)
 __global__ void kHashToHalf(const float *p, __half *ph, size_t n)
 {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        ph[i] = __float2half_rn(p[i]);
+        writePair(ph, i, __float2half_rn(p[i]));
 }
 
 // splitmix64 for parameter initialisation (host)
@@ -780,7 +855,7 @@ int guideCreate(optpt_guide *g, const float lo[3], const float hi[3], uint32_t s
     alloc((void **)&g->mlp, sizeof(float) * MLP_PARAMS);
     alloc((void **)&g->tiles, 2 * LAYERS * W_BYTES);
     alloc((void **)&g->hash, sizeof(float) * HASH_PARAMS);
-    alloc((void **)&g->hashH, sizeof(__half) * HASH_PARAMS);
+    alloc((void **)&g->hashH, sizeof(__half) * 2 * HASH_PARAMS);  // pair copy
     alloc((void **)&g->gMlp, sizeof(float) * MLP_PARAMS);
     alloc((void **)&g->gHash, sizeof(float) * HASH_PARAMS);
     alloc((void **)&g->mMlp, sizeof(float) * MLP_PARAMS);
@@ -830,8 +905,8 @@ cudaError_t guideInferQueries(const optpt_guide *g, const GuideQuery *q, uint32_
     if (n == 0)
         return cudaSuccess;
     const int tiles = (int)((n + TILE_ROWS - 1) / TILE_ROWS);
-    const int grid = std::min((tiles + 1) / 2, g->numSMs * 2);
-    kGuideInfer<QueryInput><<<grid, 256, INFER_SMEM, s>>>(guideGeom(g), g->hashH, g->tiles, QueryInput{q, n}, out,
+    const int grid = std::min((tiles + INFER_GROUPS - 1) / INFER_GROUPS, g->numSMs * OPTPT_INFER_MINB);
+    kGuideInfer<QueryInput><<<grid, INFER_THREADS, INFER_SMEM, s>>>(guideGeom(g), g->hashH, g->tiles, QueryInput{q, n}, out,
                                                           g->status);
     return cudaGetLastError();
 }
@@ -872,7 +947,7 @@ void launchGuideInfer(const optpt_guide *g, const DevScene &sc, const FrameParam
         else
             in.limit = fp.npix;
     }
-    kGuideInfer<HitInput><<<g->numSMs * 2, 256, INFER_SMEM, st>>>(
+    kGuideInfer<HitInput><<<g->numSMs * OPTPT_INFER_MINB, INFER_THREADS, INFER_SMEM, st>>>(
         guideGeom(g), g->hashH, g->tiles, in, reinterpret_cast<Packed *>(const_cast<void *>(fp.guide.mix)),
         g->status);
 }
@@ -897,6 +972,19 @@ int optpt_guide_create(const float lo[3], const float hi[3], uint32_t seed, optp
     }
     *out = g;
     return OPTPT_OK;
+}
+
+int optpt_guide_mixture_eval(const void *mixtures, uint32_t n, const float *xi, float *dirPdf, void *stream)
+{
+    if (n == 0)
+        return OPTPT_OK;
+    if (!mixtures || !dirPdf)
+        return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
+    const int grid = (int)std::min<uint32_t>((n + 255) / 256, 4096u);
+    kMixtureEval<<<grid, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const Packed *>(mixtures), n, xi,
+                                                         reinterpret_cast<float4 *>(dirPdf));
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? OPTPT_OK : optpt_internal_set_error(OPTPT_ERR_CUDA, cudaGetErrorString(e));
 }
 
 int optpt_guide_destroy(optpt_guide *g)

@@ -32,11 +32,16 @@ struct Levels {
     uint32_t dense[LEVELS];  // 1: (res+1)^3 <= TABLE, direct indexing
 };
 
+// Table entry of grid vertex (x, y, z): direct indexing on dense levels, else
+// a spatial hash. x enters both by addition, so the vertex at x + 1 is the
+// next entry (modulo the table): the inference copy of the table stores each
+// entry beside its successor and fetches both x-corners of a cell edge with
+// one 8-byte load.
 OPT_HD uint32_t cornerIndex(uint32_t x, uint32_t y, uint32_t z, uint32_t res1, bool dense)
 {
     if (dense)
         return x + res1 * (y + res1 * z);
-    return (x * 1u ^ y * 2654435761u ^ z * 805459861u) & (TABLE - 1u);
+    return (x + (y * 2654435761u ^ z * 805459861u)) & (TABLE - 1u);
 }
 
 // Trilinear corner c (bit 0 = x, 1 = y, 2 = z) of level `l` for a position
@@ -67,6 +72,29 @@ OPT_HD void levelCorners(const Levels &L, int l, float px, float py, float pz, u
         w[c] = ((c & 1) ? tx : 1.0f - tx) * (((c >> 1) & 1) ? ty : 1.0f - ty) * (((c >> 2) & 1) ? tz : 1.0f - tz);
         entry[c] = cornerIndex(x0 + (c & 1), y0 + ((c >> 1) & 1), z0 + ((c >> 2) & 1), res1, dense);
     }
+}
+
+// The same cell without the weights: the 8 corner entries and the fractions
+// (tx, ty, tz), from which cornerWeight forms corner c's weight with
+// levelCorners' arithmetic, at the point of use.
+OPT_HD void levelCell(const Levels &L, int l, float px, float py, float pz, uint32_t (&entry)[8], float &tx,
+                      float &ty, float &tz)
+{
+    const float r = L.res[l];
+    const float gx = px * r, gy = py * r, gz = pz * r;
+    const float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    tx = gx - fx;
+    ty = gy - fy;
+    tz = gz - fz;
+    const uint32_t x0 = (uint32_t)fx, y0 = (uint32_t)fy, z0 = (uint32_t)fz, res1 = (uint32_t)r + 1u;
+    const bool dense = L.dense[l] != 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        entry[c] = cornerIndex(x0 + (c & 1), y0 + ((c >> 1) & 1), z0 + ((c >> 2) & 1), res1, dense);
+}
+OPT_HD float cornerWeight(int c, float tx, float ty, float tz)
+{
+    return ((c & 1) ? tx : 1.0f - tx) * (((c >> 1) & 1) ? ty : 1.0f - ty) * (((c >> 2) & 1) ? tz : 1.0f - tz);
 }
 
 // ------------------------------------------------------------------ vMF mixture
@@ -173,11 +201,20 @@ OPT_D float packedHalf(const Packed &p, int i)  // i: a constant after unrolling
     const uint32_t w = wi == 0 ? q.x : wi == 1 ? q.y : wi == 2 ? q.z : q.w;
     return __half2float(__ushort_as_half((unsigned short)((i & 1) ? (w >> 16) : (w & 0xFFFFu))));
 }
+// Unit mean direction from a lobe's halves: r / |r| by one reciprocal square
+// root ((0, 0, 1) for a null lobe). Sampling and evaluation both use it, so
+// the density evaluated is the one sampled from.
+OPT_D float3 unitMu(float rx, float ry, float rz)
+{
+    const float d2 = rx * rx + ry * ry + rz * rz;
+    if (!(d2 > 1e-12f))
+        return mk3(0.0f, 0.0f, 1.0f);
+    const float il = rsqrtf(d2);
+    return mk3(rx * il, ry * il, rz * il);
+}
 OPT_D float3 packedMu(const Packed &p, int k)
 {
-    const float3 r = mk3(packedHalf(p, 4 * k), packedHalf(p, 4 * k + 1), packedHalf(p, 4 * k + 2));
-    const float len = sqrtf(dot3(r, r));
-    return len > 1e-6f ? r * (1.0f / len) : mk3(0.0f, 0.0f, 1.0f);
+    return unitMu(packedHalf(p, 4 * k), packedHalf(p, 4 * k + 1), packedHalf(p, 4 * k + 2));
 }
 OPT_D float packedSelect(const Packed &p) { return packedHalf(p, 40); }
 OPT_D float packedWeightSum(const Packed &p)
@@ -192,9 +229,16 @@ OPT_D float packedWeight(const Packed &p, int k, float sum, float inv)
 {
     return sum > 0.0f ? packedHalf(p, 32 + k) * inv : 1.0f / LOBES;
 }
-OPT_D float vmfPdfAt(float3 mu, float kappa, float3 w)
+// vMF density of a packed lobe with the hardware exponential: a packed kappa
+// is 0 (null mixture: isotropic) or exp(log kappa) >= exp(LOG_KAPPA_MIN)
+// ~ 0.05, where 1 - exp(-2 kappa) >= 0.095, so the subtraction keeps a
+// relative error near 1e-6 without expm1.
+OPT_D float vmfPdfPacked(float3 mu, float kappa, float3 w)
 {
-    return vmfNorm(kappa) * expf(kappa * (dot3(mu, w) - 1.0f));
+    if (kappa < 1e-4f)
+        return 0.25f * OPT_INV_PI;
+    const float norm = __fdividef(kappa * (0.5f * OPT_INV_PI), 1.0f - __expf(-2.0f * kappa));
+    return norm * __expf(kappa * (dot3(mu, w) - 1.0f));
 }
 OPT_D float mixturePdf(const Packed &p, float3 w)
 {
@@ -202,7 +246,7 @@ OPT_D float mixturePdf(const Packed &p, float3 w)
     float pdf = 0.0f;
 #pragma unroll
     for (int k = 0; k < LOBES; ++k)
-        pdf += packedWeight(p, k, sum, inv) * vmfPdfAt(packedMu(p, k), packedHalf(p, 4 * k + 3), w);
+        pdf += packedWeight(p, k, sum, inv) * vmfPdfPacked(packedMu(p, k), packedHalf(p, 4 * k + 3), w);
     return pdf;
 }
 // Lobe by xi0 over the weights, then a direction from it.
@@ -220,8 +264,7 @@ OPT_D float3 mixtureSample(const Packed &p, float xi0, float xi1, float xi2)
             found = true;
         }
     }
-    // the chosen lobe's halves first, then one normalisation (packedMu's
-    // arithmetic on them)
+    // the chosen lobe's halves first, then one normalisation (packedMu's)
     float rx = packedHalf(p, 4 * (LOBES - 1)), ry = packedHalf(p, 4 * (LOBES - 1) + 1),
           rz = packedHalf(p, 4 * (LOBES - 1) + 2), kappa = packedHalf(p, 4 * (LOBES - 1) + 3);
 #pragma unroll
@@ -232,10 +275,7 @@ OPT_D float3 mixtureSample(const Packed &p, float xi0, float xi1, float xi2)
             rz = packedHalf(p, 4 * j + 2);
             kappa = packedHalf(p, 4 * j + 3);
         }
-    const float3 r = mk3(rx, ry, rz);
-    const float len = sqrtf(dot3(r, r));
-    const float3 mu = len > 1e-6f ? r * (1.0f / len) : mk3(0.0f, 0.0f, 1.0f);
-    return vmfSample(mu, kappa, xi1, xi2);
+    return vmfSample(unitMu(rx, ry, rz), kappa, xi1, xi2);
 }
 
 }  // namespace guide

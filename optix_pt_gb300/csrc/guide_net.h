@@ -12,7 +12,7 @@ struct optpt_guide {
     float *mlp = nullptr;     // [LAYERS][64 out][64 in]
     uint8_t *tiles = nullptr; // 2 * LAYERS tiles of 8 KB: W_l (rows out) then W_l^T (rows in)
     float *hash = nullptr;    // [LEVELS][TABLE][FEATS]
-    __half *hashH = nullptr;
+    __half *hashH = nullptr;  // FP16 pair copy: slot e = (entry e, entry e + 1) of its level
     // gradients and Adam moments
     float *gMlp = nullptr, *gHash = nullptr;
     float *mMlp = nullptr, *vMlp = nullptr, *mHash = nullptr, *vHash = nullptr;

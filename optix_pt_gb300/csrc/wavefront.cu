@@ -711,8 +711,13 @@ OPT_D void shadeRay(const DevScene &s, const FrameParams &fp, const WaveBufs &q,
 // (measured on the 1080p sweep: 1.43 -> 1.27 ms per pass at 64 registers,
 // 96 and 80 in between; with one copy of each BSDF lobe, 72 is 0.9 % ahead
 // of 64 on the sweep and 56 behind).
+// The guided variant (mixture reads, sampling and densities) has its own cap.
+#ifndef OPTPT_SHADE_GUIDED_REGS
+#define OPTPT_SHADE_GUIDED_REGS 72
+#endif
 template <bool GUIDED, bool BLOCKPUSH>
-__global__ void __maxnreg__(72) kShade(DevScene s, FrameParams fp, WaveBufs q, int depth)
+__global__ void __maxnreg__(GUIDED ? OPTPT_SHADE_GUIDED_REGS : 72) kShade(DevScene s, FrameParams fp, WaveBufs q,
+                                                                         int depth)
 {
     const uint32_t count = q.counters[CNT_EXT + depth];
     const int lane = threadIdx.x & 31;

@@ -6,7 +6,7 @@ GPU implements, used to check its forward pass and gradients.
 * Multiresolution hash-grid encoding (Mueller et al., "Instant Neural Graphics
   Primitives", SIGGRAPH 2022): 16 levels x 2 features, 2^19 entries per level,
   dense indexing where (res + 1)^3 fits the table, else the spatial hash
-  x * 1 ^ y * 2654435761 ^ z * 805459861 (mod 2^19); trilinear weights.
+  x + (y * 2654435761 ^ z * 805459861) (mod 2^19); trilinear weights.
 * MLP 64 -> 64 -> 64 -> 64 -> 64 -> 64 (ReLU, no biases; a constant-1 input),
   BF16 operands with FP32 accumulation: every matrix operand is rounded to
   BF16 (round to nearest even) exactly where the tensor-core kernels round.
@@ -60,7 +60,7 @@ def corners(levels_res, levels_dense, lo, inv_ext, pos):
                 e = x + res1 * (y + res1 * z)
             else:
                 m = np.uint64(0xFFFFFFFF)
-                e = ((x & m) ^ ((y * np.uint64(2654435761)) & m) ^ ((z * np.uint64(805459861)) & m)) & np.uint64(
+                e = (x + (((y * np.uint64(2654435761)) & m) ^ ((z * np.uint64(805459861)) & m))) & np.uint64(
                     TABLE - 1)
             ent[:, l, c] = e.astype(np.int64)
     return ent, wts

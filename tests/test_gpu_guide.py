@@ -201,3 +201,102 @@ def test_guide_training_learns_a_directional_target(cuda_dev):
     assert after > before + 2.0
     assert after > np.log(20 / (2 * np.pi)) - 1.5   # near the target lobe's own peak density (log 1.16)
     g.close()
+
+
+def _packed(mu, kap, w, select=0.5):
+    """Rows of packed mixtures (n, 48) float16 from per-row lobes."""
+    n = mu.shape[0]
+    lobes = np.zeros((n, 8, 4))
+    lobes[:, :, :3] = mu
+    lobes[:, :, 3] = kap
+    h = np.zeros((n, 48), np.float16)
+    h[:, :32] = lobes.reshape(n, 32)
+    h[:, 32:40] = w
+    h[:, 40] = select
+    return h
+
+
+def test_mixture_sampler_matches_its_density(cuda_dev):
+    """The shading kernel's mixture sampler and density (the same device
+    functions, through optpt_guide_mixture_eval): the density equals the FP64
+    vMF mixture of the decoded halves; the sampled directions follow it
+    (per-lobe Kolmogorov-Smirnov test of mu . d against the vMF's own CDF,
+    uniform azimuth, and lobe-selection frequencies equal to the weights).
+    A guided vertex's one-sample MIS weight is unbiased only if the density
+    it evaluates is the one its sampler draws from."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    from oracle import guide_oracle as go
+    rng = np.random.default_rng(21)
+    n = 4096
+    mu = _unit(rng, n * 8).reshape(n, 8, 3) * rng.uniform(0.5, 2.0, (n, 8, 1))
+    kap = np.exp(rng.uniform(-3.0, 5.5, (n, 8)))
+    w = rng.uniform(0.0, 1.0, (n, 8))
+    h = _packed(mu, kap, w)
+    mix = torch.from_numpy(h.view(np.int16)).to(cuda_dev)
+    wd, mud, kapd = go.unpack(h)
+    dirs = _unit(rng, n)
+    dp = torch.from_numpy(np.concatenate([dirs, np.zeros((n, 1))], 1).astype(np.float32)).to(cuda_dev)
+    opt.Guide.mixture_eval(mix.data_ptr(), n, None, dp.data_ptr(), torch.cuda.current_stream())
+    xi = torch.from_numpy(rng.uniform(0.0, 1.0, (n, 3)).astype(np.float32)).to(cuda_dev)
+    ds = torch.zeros((n, 4), dtype=torch.float32, device=cuda_dev)
+    opt.Guide.mixture_eval(mix.data_ptr(), n, xi.data_ptr(), ds.data_ptr(), torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    for d, got in ((dirs, dp.cpu().numpy()[:, 3]), (ds.cpu().numpy()[:, :3].astype(np.float64), ds.cpu().numpy()[:, 3])):
+        ref = (wd * go.vmf_pdf(mud, kapd, d)[0]).sum(1)
+        ok = ref > 1e-30
+        rel = np.abs(got[ok] - ref[ok]) / ref[ok]
+        print("mixture density rel err: median %.2e max %.2e" % (np.median(rel), rel.max()))
+        assert np.median(rel) < 2e-6 and rel.max() < 1e-4
+    assert np.abs(np.linalg.norm(ds.cpu().numpy()[:, :3], axis=1) - 1).max() < 1e-5
+
+    # one-lobe mixtures: mu . d against F(t) = (exp(k (t - 1)) - exp(-2 k)) / (1 - exp(-2 k))
+    R = 1 << 16
+    for k in (0.05, 1.0, 10.0, 200.0):
+        m = _unit(rng, 1)
+        mu1 = np.zeros((R, 8, 3))
+        mu1[:, 0] = m
+        mu1[:, 1:, 2] = 1.0
+        w1 = np.zeros((R, 8))
+        w1[:, 0] = 1.0
+        h1 = _packed(mu1, np.full((R, 8), k), w1)
+        kd = float(h1[0, 3])
+        mix1 = torch.from_numpy(h1.view(np.int16)).to(cuda_dev)
+        xi1 = torch.from_numpy(rng.uniform(0.0, 1.0, (R, 3)).astype(np.float32)).to(cuda_dev)
+        out = torch.zeros((R, 4), dtype=torch.float32, device=cuda_dev)
+        opt.Guide.mixture_eval(mix1.data_ptr(), R, xi1.data_ptr(), out.data_ptr(), torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        d = out.cpu().numpy()[:, :3].astype(np.float64)
+        mh = go.unpack(h1[:1])[1][0, 0]
+        t = np.clip(d @ mh, -1.0, 1.0)
+        ts = np.sort(t)
+        cdf = (np.exp(kd * (ts - 1)) - np.exp(-2 * kd)) / -np.expm1(-2 * kd)
+        ks = max(np.abs(cdf - np.arange(1, R + 1) / R).max(), np.abs(cdf - np.arange(R) / R).max())
+        # azimuth about mu: uniform
+        a = np.cross(mh, [0.0, 0.0, 1.0] if abs(mh[2]) < 0.9 else [1.0, 0.0, 0.0])
+        a /= np.linalg.norm(a)
+        b = np.cross(mh, a)
+        phi = np.sort((np.arctan2(d @ b, d @ a) + np.pi) / (2 * np.pi))
+        ks_phi = np.abs(phi - (np.arange(R) + 0.5) / R).max()
+        print("kappa %g: KS(mu.d) %.4f, KS(azimuth) %.4f" % (kd, ks, ks_phi))
+        assert ks < 1.95 / np.sqrt(R) and ks_phi < 1.95 / np.sqrt(R), (kd, ks, ks_phi)
+
+    # lobe selection: eight peaked, well separated lobes; the nearest lobe of
+    # each draw is the one selected
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [0.577, 0.577, 0.577], [-0.577, -0.577, 0.577]])
+    wsel = rng.uniform(0.2, 1.0, 8)
+    h2 = _packed(np.broadcast_to(axes, (R, 8, 3)), np.full((R, 8), 200.0), np.broadcast_to(wsel, (R, 8)))
+    mix2 = torch.from_numpy(h2.view(np.int16)).to(cuda_dev)
+    xi2 = torch.from_numpy(rng.uniform(0.0, 1.0, (R, 3)).astype(np.float32)).to(cuda_dev)
+    out = torch.zeros((R, 4), dtype=torch.float32, device=cuda_dev)
+    opt.Guide.mixture_eval(mix2.data_ptr(), R, xi2.data_ptr(), out.data_ptr(), torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    wd2, mud2, _ = go.unpack(h2[:1])
+    lobe = np.argmax(out.cpu().numpy()[:, :3].astype(np.float64) @ mud2[0].T, axis=1)
+    counts = np.bincount(lobe, minlength=8)
+    expect = wd2[0] * R
+    chi2 = float(((counts - expect) ** 2 / expect).sum())
+    print("lobe selection chi2 %.2f (7 dof)" % chi2)
+    assert chi2 < 24.3   # p = 0.001 for 7 degrees of freedom

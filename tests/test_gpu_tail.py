@@ -67,9 +67,11 @@ def test_tail_kernel_in_batched_views(cuda_dev):
 
 def test_tail_kernel_past_the_guided_bounces(cuda_dev):
     """With guiding on, the path-completion kernel takes over only past the
-    guided bounces (from the guiding maxDepth + 2 on: bounce maxDepth + 1
-    still completes a training path's last record); a tail bounce inside the
-    guided range is ignored. Online training adds hash-grid gradients with
+    guided bounces: a tail bounce inside the guided range is raised to the
+    guiding maxDepth + 1, or + 2 while the network trains (bounce maxDepth + 1
+    then still completes a training path's last record). The renders train
+    for their first half and run frozen for the second, so both limits are
+    exercised. Online training adds hash-grid gradients with
     atomics, in no fixed order, so two guided renders differ in rounding even
     with the same settings; the renders are therefore compared statistically
     (per-pixel z scores of the difference and the frame mean) with the
@@ -84,7 +86,7 @@ def test_tail_kernel_past_the_guided_bounces(cuda_dev):
         r = opt.Renderer(sc, spp_batch=16, tail_bounce=tail)
         r.setupOutputBuffer(48, 48)
         r.set_guiding(1)
-        r.guiding_options(maxDepth=3)
+        r.guiding_options(maxDepth=3, trainSpp=256)
         r.render(512, torch.cuda.current_stream())
         torch.cuda.synchronize()
         s, q, n = r.accum()
