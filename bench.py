@@ -63,9 +63,10 @@ GUIDED = {"workload": "indirect-lit interior (doorway only), 1,947,146 tris, dep
           # (one path in two records; 512 passes of 2 spp, each with 4 Adam
           # steps), then the network is frozen; mixture selection probability
           # capped at 0.6; the first 6 bounces guided, the path-completion
-          # kernel from bounce 8 on (plain: from bounce 5, the default)
+          # kernel from bounce 7 on (from bounce 8 while the network trains;
+          # plain: from bounce 5, the default)
           "guiding_options": {"trainSpp": 1024, "trainStride": 2, "alphaMax": 0.6, "maxDepth": 6},
-          "guided_tail_bounce": 8}
+          "guided_tail_bounce": 7}
 BATCH = {"workload": "batched multi-view: 96 views (48 of the terrain, 48 of the material sweep), sides "
                      "log-uniform 128..1024, spp U{16..256}, depth 12, guiding on; both scenes in one multi-scene "
                      "batch, each scene's renderer autotuned with guiding on (leaf size, block size, compaction)",
