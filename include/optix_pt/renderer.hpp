@@ -113,6 +113,21 @@ class Renderer {
         check(optpt_setup_camera(h_, cam.eye, cam.target, cam.upHint, cam.vertFovDeg), "updateLaunchParams");
     }
     void launch() { check(optpt_launch(h_), "launch"); }
+    // Frame loop without a stall per frame: renders a frame and returns the
+    // previous one (its download overlapped this frame's render); nullptr
+    // on the first call. launchFlush() returns the last frame.
+    const float *launchPipelined()
+    {
+        const float *f = nullptr;
+        check(optpt_launch_pipelined(h_, &f), "launchPipelined");
+        return f;
+    }
+    const float *launchFlush()
+    {
+        const float *f = nullptr;
+        check(optpt_launch_flush(h_, &f), "launchFlush");
+        return f;
+    }
 
     void *getFrameBuffer() { return (void *)optpt_get_frame_buffer(h_); }
     uint32_t getSampleCount() { return optpt_get_sample_count(h_); }

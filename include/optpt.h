@@ -247,6 +247,19 @@ int optpt_render(optpt_renderer *r, uint32_t spp, void *stream);
  * tone-mapped frame buffer to the renderer's host buffer. */
 int optpt_launch(optpt_renderer *r);
 
+/* Renderer::launch (src/renderer.cpp:940-958) as a pipelined frame loop:
+ * renders one frame (1 spp, as optpt_launch), snapshots its tone-mapped
+ * frame buffer on the device and copies it to pinned host memory on a copy
+ * stream, so the copy overlaps the next frame's rendering instead of
+ * following it. *frame receives the previous call's frame, complete in host
+ * memory (NULL on the first call after a flush or a resize);
+ * optpt_launch_flush waits for the last frame's copy and hands it out. The
+ * frames are float4 w*h in two pinned buffers owned by the renderer; one
+ * stays valid until the second pipelined call after the one that returned
+ * it. Frames are bit-identical to optpt_launch's. */
+int optpt_launch_pipelined(optpt_renderer *r, const float **frame);
+int optpt_launch_flush(optpt_renderer *r, const float **frame);
+
 /* Renderer::getFrameBuffer (src/renderer.cpp:1344): host float4 w*h owned
  * by the renderer, valid after optpt_launch. NULL before. */
 const float *optpt_get_frame_buffer(optpt_renderer *r);

@@ -334,6 +334,28 @@ class Renderer:
         """1 sample per pixel, wait, copy the frame buffer to host (src/renderer.cpp:940-958)."""
         check(lib.optpt_launch(self._h))
 
+    def _frame_view(self, p, copy):
+        if not p:
+            return None
+        lp = self.launch_params()
+        a = np.ctypeslib.as_array(p, shape=(lp.h, lp.w, 4))
+        return a.copy() if copy else a
+
+    def launch_pipelined(self, copy=True):
+        """launch() as a pipelined frame loop: renders a frame and starts its
+        copy to host memory; returns the previous call's frame (None after a
+        flush or a resize). With copy=False the array is a view of the
+        renderer's pinned buffer, valid until the second call after."""
+        p = ctypes.POINTER(ctypes.c_float)()
+        check(lib.optpt_launch_pipelined(self._h, ctypes.byref(p)))
+        return self._frame_view(p, copy)
+
+    def launch_flush(self, copy=True):
+        """The last pipelined frame, once its copy has finished (None if none is pending)."""
+        p = ctypes.POINTER(ctypes.c_float)()
+        check(lib.optpt_launch_flush(self._h, ctypes.byref(p)))
+        return self._frame_view(p, copy)
+
     def getFrameBuffer(self):
         p = lib.optpt_get_frame_buffer(self._h)
         if not p:

@@ -212,6 +212,8 @@ _sigs = {
     "optpt_set_launch_params": (ctypes.c_int, [_H, ctypes.POINTER(LaunchParams)]),
     "optpt_render": (ctypes.c_int, [_H, ctypes.c_uint32, _P]),
     "optpt_launch": (ctypes.c_int, [_H]),
+    "optpt_launch_pipelined": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.POINTER(ctypes.c_float))]),
+    "optpt_launch_flush": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.POINTER(ctypes.c_float))]),
     "optpt_get_frame_buffer": (ctypes.POINTER(ctypes.c_float), [_H]),
     "optpt_get_sample_count": (ctypes.c_uint32, [_H]),
     "optpt_reset_sample_count": (ctypes.c_int, [_H]),

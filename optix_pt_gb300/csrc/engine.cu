@@ -78,6 +78,18 @@ struct optpt_renderer {
     LaunchShape shape{};
     std::vector<float> hostFb;
     bool hostFbValid = false;
+    // Pipelined launches (optpt_launch_pipelined): a frame's tone-mapped
+    // buffer is snapshot on the device and copied to pinned host memory on a
+    // copy stream while the next frame renders; two slots alternate.
+    struct FramePipe {
+        float4 *stage[2] = {nullptr, nullptr};
+        float *host[2] = {nullptr, nullptr};
+        cudaEvent_t staged[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+        cudaStream_t copyStream = nullptr;
+        size_t pixels = 0;
+        uint32_t next = 0;  // slot of the next frame
+        int pending = -1;   // slot whose copy is in flight, -1 = none
+    } pipe;
     void *outScratch = nullptr;  // device payloads of optpt_read_rgba8 / optpt_save_image
     size_t outScratchBytes = 0;
 
@@ -102,6 +114,14 @@ struct optpt_renderer {
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
 
     FrameConst *dFrameConst = nullptr;
+    // Frame constants go up from a small pinned ring: an upload from pageable
+    // memory may wait for the stream's earlier work (the driver stages it),
+    // which would leave the GPU idle while the host enqueues the next frame.
+    // A slot is rewritten only after its previous copy has run.
+    static constexpr int FC_SLOTS = 4;
+    FrameConst *hFrameConst = nullptr;  // pinned, FC_SLOTS entries
+    cudaEvent_t fcCopied[FC_SLOTS] = {};
+    uint32_t fcNext = 0;
 
     // learned guiding (mode 0 off, 1 guided + online training, 2 guided, frozen)
     optpt_guide *guide = nullptr;
@@ -209,6 +229,20 @@ struct optpt_renderer {
         gMixPaths = gRecSlots = 0;
     }
 
+    cudaError_t uploadFrameConst(cudaStream_t st)
+    {
+        const uint32_t k = fcNext;
+        fcNext = (k + 1) % FC_SLOTS;
+        cudaError_t e = cudaEventSynchronize(fcCopied[k]);  // returns at once if never recorded
+        if (e != cudaSuccess)
+            return e;
+        hFrameConst[k] = frameConst();
+        if ((e = cudaMemcpyAsync(dFrameConst, hFrameConst + k, sizeof(FrameConst), cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess)
+            return e;
+        return cudaEventRecord(fcCopied[k], st);
+    }
+
     FrameConst frameConst() const
     {
         auto bits = [](uint32_t u) {
@@ -226,8 +260,27 @@ struct optpt_renderer {
         return c;
     }
 
+    void freePipe()
+    {
+        if (pipe.copyStream)
+            cudaStreamSynchronize(pipe.copyStream);
+        for (int k = 0; k < 2; ++k) {
+            cudaFree(pipe.stage[k]);
+            if (pipe.host[k])
+                cudaFreeHost(pipe.host[k]);
+            if (pipe.staged[k])
+                cudaEventDestroy(pipe.staged[k]);
+            if (pipe.copied[k])
+                cudaEventDestroy(pipe.copied[k]);
+        }
+        if (pipe.copyStream)
+            cudaStreamDestroy(pipe.copyStream);
+        pipe = FramePipe{};
+    }
+
     void freeFrame()
     {
+        freePipe();
         if (graphExec)
             cudaGraphExecDestroy(graphExec);
         if (graph)
@@ -270,6 +323,11 @@ struct optpt_renderer {
         cudaFree(q.counters);
         cudaFree(dState);
         cudaFree(dFrameConst);
+        if (hFrameConst)
+            cudaFreeHost(hFrameConst);
+        for (auto &e : fcCopied)
+            if (e)
+                cudaEventDestroy(e);
         freeBvh(bvh);
         cudaFree(dPositions);
         cudaFree(dNormals);
@@ -875,8 +933,17 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
             (e = cudaMemset(r->q.totals, 0, sizeof(unsigned long long) * TOTALS_COUNT)) ||
             (e = cudaMalloc((void **)&r->dState, sizeof(uint32_t) * 4)) ||
             (e = cudaMemset(r->dState, 0, sizeof(uint32_t) * 4)) ||
-            (e = cudaMalloc((void **)&r->dFrameConst, sizeof(FrameConst)))) {
+            (e = cudaMalloc((void **)&r->dFrameConst, sizeof(FrameConst))) ||
+            (e = cudaHostAlloc((void **)&r->hFrameConst, sizeof(FrameConst) * optpt_renderer::FC_SLOTS,
+                               cudaHostAllocDefault))) {
             rc = cudaFail(e, "counters");
+            break;
+        }
+        for (auto &ev : r->fcCopied)
+            if (!e)
+                e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e) {
+            rc = cudaFail(e, "events");
             break;
         }
         // Frame contract defaults (src/renderer.cpp:24-60, include/renderer.h:137-146).
@@ -1000,8 +1067,7 @@ int batchSetup(optpt_renderer *r, const optpt_view *views, uint32_t numViews, cu
     CUDA_OR_RETURN(cudaMemsetAsync(B.acc.sum, 0, sizeof(Acc4) * B.totalPixels, st), "batch");
     CUDA_OR_RETURN(cudaMemsetAsync(B.acc.sumSq, 0, sizeof(Acc4) * B.totalPixels, st), "batch");
     B.done.assign(numViews, 0u);
-    const FrameConst fc = r->frameConst();
-    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    CUDA_OR_RETURN(r->uploadFrameConst(st), "frame constants");
 
     FrameParams fp = r->frameParams();
     fp.w = fp.h = fp.npix = fp.sppBatch = 0;
@@ -1456,11 +1522,10 @@ int optpt_render(optpt_renderer *r, uint32_t spp, void *stream)
     if (rc)
         return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    // The frame constants go up first (from pageable memory, so the host copy
-    // may change as soon as this returns). Whole passes of sppBatch samples
-    // replay the captured graph; a remainder runs as one smaller pass.
-    const FrameConst fc = r->frameConst();
-    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    // The frame constants go up first (from the pinned ring, so the host
+    // copy may change as soon as this returns). Whole passes of sppBatch
+    // samples replay the captured graph; a remainder runs as one smaller pass.
+    CUDA_OR_RETURN(r->uploadFrameConst(st), "frame constants");
     if ((rc = ensureGuideBuffers(r)))
         return rc;
     const uint32_t passes = spp / r->sppBatch, rem = spp % r->sppBatch;
@@ -1507,6 +1572,74 @@ int optpt_launch(optpt_renderer *r)
                    "frame buffer copy");
     CUDA_OR_RETURN(cudaStreamSynchronize(r->ownStream), "launch");
     r->hostFbValid = true;
+    return OPTPT_OK;
+}
+
+int optpt_launch_pipelined(optpt_renderer *r, const float **frame)
+{
+    if (frame)
+        *frame = nullptr;
+    int rc = checkRenderable(r);
+    if (rc)
+        return rc;
+    if (!frame)
+        return fail(OPTPT_ERR_INVALID, "frame is NULL");
+    auto &P = r->pipe;
+    const size_t npix = (size_t)r->w * r->h, bytes = sizeof(float4) * npix;
+    if (P.pixels != npix) {
+        r->freePipe();
+        cudaError_t e = cudaStreamCreateWithFlags(&P.copyStream, cudaStreamNonBlocking);
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+            e = cudaMalloc((void **)&P.stage[k], bytes);
+            if (e == cudaSuccess)
+                e = cudaHostAlloc((void **)&P.host[k], bytes, cudaHostAllocDefault);
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(&P.staged[k], cudaEventDisableTiming);
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(&P.copied[k], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) {
+            r->freePipe();
+            return cudaFail(e, "pipelined frame buffers");
+        }
+        P.pixels = npix;
+    }
+    const uint32_t k = P.next;
+    if ((rc = optpt_render(r, 1, r->ownStream)))
+        return rc;
+    // The snapshot reuses slot k: the copy made from it two frames ago must
+    // have finished (a wait on an event never recorded returns at once).
+    CUDA_OR_RETURN(cudaStreamWaitEvent(r->ownStream, P.copied[k], 0), "pipelined launch");
+    launchCopyFrame(r->acc.frameBuffer, P.stage[k], npix, r->ownStream);
+    CUDA_OR_RETURN(cudaGetLastError(), "frame snapshot");
+    CUDA_OR_RETURN(cudaEventRecord(P.staged[k], r->ownStream), "pipelined launch");
+    CUDA_OR_RETURN(cudaStreamWaitEvent(P.copyStream, P.staged[k], 0), "pipelined launch");
+    CUDA_OR_RETURN(cudaMemcpyAsync(P.host[k], P.stage[k], bytes, cudaMemcpyDeviceToHost, P.copyStream),
+                   "frame copy");
+    CUDA_OR_RETURN(cudaEventRecord(P.copied[k], P.copyStream), "pipelined launch");
+    const int prev = P.pending;
+    P.pending = (int)k;
+    P.next = k ^ 1u;
+    if (prev >= 0) {
+        CUDA_OR_RETURN(cudaEventSynchronize(P.copied[prev]), "frame copy");
+        *frame = P.host[prev];
+    }
+    return OPTPT_OK;
+}
+
+int optpt_launch_flush(optpt_renderer *r, const float **frame)
+{
+    if (frame)
+        *frame = nullptr;
+    if (!r || !frame)
+        return fail(OPTPT_ERR_INVALID, "NULL argument");
+    auto &P = r->pipe;
+    if (P.pending < 0)
+        return OPTPT_OK;
+    const int k = P.pending;
+    P.pending = -1;
+    CUDA_OR_RETURN(cudaEventSynchronize(P.copied[k]), "frame copy");
+    *frame = P.host[k];
     return OPTPT_OK;
 }
 
@@ -1901,8 +2034,7 @@ int optpt_render_profiled(optpt_renderer *r, uint32_t spp, void *stream, optpt_k
     for (auto &e : ev)
         CUDA_OR_RETURN(cudaEventCreate(&e), "event");
     unsigned long long before[2] = {0, 0}, after[2] = {0, 0};
-    const FrameConst fc = r->frameConst();
-    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    CUDA_OR_RETURN(r->uploadFrameConst(st), "frame constants");
     CUDA_OR_RETURN(cudaStreamSynchronize(st), "profile");
     CUDA_OR_RETURN(cudaMemcpy(before, r->q.totals, sizeof(before), cudaMemcpyDeviceToHost), "profile");
     const uint32_t passes = (spp + r->sppBatch - 1) / r->sppBatch;
@@ -1942,8 +2074,7 @@ int optpt_traversal_counts(optpt_renderer *r, uint32_t spp, void *stream, optpt_
         return rc;
     cudaStream_t st = (cudaStream_t)stream;
     unsigned long long before[8], after[8];
-    const FrameConst fc = r->frameConst();
-    CUDA_OR_RETURN(cudaMemcpyAsync(r->dFrameConst, &fc, sizeof(fc), cudaMemcpyHostToDevice, st), "frame constants");
+    CUDA_OR_RETURN(r->uploadFrameConst(st), "frame constants");
     CUDA_OR_RETURN(cudaStreamSynchronize(st), "counts");
     CUDA_OR_RETURN(cudaMemcpy(before, r->q.totals, sizeof(before), cudaMemcpyDeviceToHost), "counts");
     const FrameParams fp = r->frameParams();

@@ -206,6 +206,7 @@ void launchFinish(const LaunchShape &ls, const DevScene &s, const FrameParams &f
 void launchAccumulate(const LaunchShape &ls, const FrameParams &fp, const WaveBufs &q, const AccumBufs &a,
                       cudaStream_t st);
 void launchAdvance(const FrameParams &fp, uint32_t *state, cudaStream_t st);
+void launchCopyFrame(const float4 *src, float4 *dst, size_t n, cudaStream_t st);
 // Traversal faults of the traced rays are added to totals[8], totals[9].
 void launchTrace(const DevScene &s, const float4 *rays, float4 *hits, uint32_t n, int anyHit,
                  unsigned long long *totals, cudaStream_t st);

@@ -992,6 +992,14 @@ __global__ void __launch_bounds__(256) kAccumulate(FrameParams fp, WaveBufs q, A
 // Advances the sample counter after a pass (one thread).
 // state[0]: samples accumulated (reset with the accumulator); state[1]: passes
 // run by this renderer (never reset; stamps guiding records).
+// The pipelined frame loop's device snapshot of the frame buffer, by the
+// SMs at HBM speed (it sits between two frames' passes on the stream).
+__global__ void kCopyFrame(const float4 *__restrict__ src, float4 *__restrict__ dst, size_t n)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = __ldcs(src + i);
+}
+
 __global__ void kAdvance(uint32_t *state, uint32_t by)
 {
     state[0] += by;
@@ -1152,6 +1160,14 @@ void launchAccumulate(const LaunchShape &ls, const FrameParams &fp, const WaveBu
                       cudaStream_t st)
 {
     kAccumulate<<<ls.gridAccum, ls.block, 0, st>>>(fp, q, a);
+}
+void launchCopyFrame(const float4 *src, float4 *dst, size_t n, cudaStream_t st)
+{
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t blocks = (n + 255) / 256, cap = (size_t)sms * 8;
+    kCopyFrame<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(src, dst, n);
 }
 void launchAdvance(const FrameParams &fp, uint32_t *state, cudaStream_t st)
 {

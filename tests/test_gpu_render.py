@@ -206,6 +206,38 @@ def test_launch_and_framebuffer_match_tonemapped_mean(cuda_dev):
     r.close()
 
 
+def test_pipelined_launch_frames_match_synchronous_launch(cuda_dev):
+    """optpt_launch_pipelined hands out each frame one call late, complete in
+    host memory and bit-identical to optpt_launch's frame; optpt_launch_flush
+    hands out the last one; a resize drops the pending frame and the loop
+    starts again."""
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    a = opt.Renderer(sc)
+    a.setupOutputBuffer(64, 48)
+    want = []
+    for _ in range(5):
+        a.launch()
+        want.append(a.getFrameBuffer())
+    a.close()
+    b = opt.Renderer(sc)
+    b.setupOutputBuffer(64, 48)
+    got = [b.launch_pipelined() for _ in range(5)]
+    assert got[0] is None
+    got = got[1:] + [b.launch_flush()]
+    assert b.launch_flush() is None
+    assert b.getSampleCount() == 5
+    for k, (x, y) in enumerate(zip(want, got)):
+        assert np.array_equal(x, y), k
+    assert not np.array_equal(want[0], want[4])   # the frames do differ from one another
+    b.launch_pipelined()
+    b.setupOutputBuffer(32, 16)
+    assert b.launch_pipelined() is None
+    f = b.launch_flush()
+    assert f.shape == (16, 32, 4) and np.isfinite(f).all() and f.any()
+    b.close()
+
+
 def test_visualisation_albedo(cuda_dev):
     import optix_pt_gb300 as opt
     sc = opt.Scene.procedural("cornell")
