@@ -69,7 +69,7 @@ GUIDED = {"workload": "indirect-lit interior (doorway only), 1,947,146 tris, dep
           "guided_tail_bounce": 7}
 BATCH = {"workload": "batched multi-view: 96 views (48 of the terrain, 48 of the material sweep), sides "
                      "log-uniform 128..1024, spp U{16..256}, depth 12, guiding on; both scenes in one multi-scene "
-                     "batch, each scene's renderer autotuned with guiding on (leaf size, block size, compaction)",
+                     "batch, each scene's renderer autotuned with guiding on (BVH tree, block size, compaction)",
          "views_per_scene": 48, "seed": 5,
          "reference_spp_factor": 4}
 WORKLOAD = dict(WORKLOADS["sweep"])
@@ -584,8 +584,9 @@ def run_batch(stream, peak):
     for k, name in enumerate(names):
         scene = opt.Scene.procedural(name)
         best, trials = opt.autotune(scene, 320, 180, 16, guiding=1)   # timed as it renders: guided
+        builder = "ploc" if best["bvhBuilder"] == 1 else "lbvh"
         r = opt.Renderer(scene, leaf_size=best["leafSize"], block_size=best["blockSize"],
-                         compaction=best["compaction"])
+                         compaction=best["compaction"], bvh_builder=builder)
         r.set_max_depth(12)
         r.set_guiding(1)
         scenes.append(scene)
@@ -611,7 +612,7 @@ def run_batch(stream, peak):
         samples = st1[k]["pathSamples"] - st0[k]["pathSamples"]
         # One plain renderer per scene draws the references and, first, a
         # counting pass over the scene's first view for its BVH work per ray.
-        ref = opt.Renderer(scene, leaf_size=best["leafSize"])
+        ref = opt.Renderer(scene, leaf_size=best["leafSize"], bvh_builder=builder)
         ref.set_max_depth(12)
         eye, tgt, up, fov, w0, h0, _ = mine[0]
         ref.setupOutputBuffer(w0, h0)

@@ -210,6 +210,12 @@ typedef struct optpt_options {
                           * guiding maxDepth + 1 at the earliest (+ 2 while the
                           * network trains); 0 = OPTPT_DEFAULT_TAIL_BOUNCE,
                           * 0xFFFFFFFF = never                                  */
+    uint32_t bvhBuilder; /* binary tree the 8-wide BVH is collapsed from: 0 = the
+                          * LBVH (Morton radix tree, reproduced bit for bit by the
+                          * host oracle; default), 1 = PLOC clustering on the same
+                          * Morton order (leaves of one triangle, leafSize
+                          * ignored). The binary BVH (bvhWidth 2) is always the
+                          * LBVH.                                                 */
 } optpt_options;
 #define OPTPT_DEFAULT_TAIL_BOUNCE 5
 
@@ -511,7 +517,8 @@ int optpt_guide_status(optpt_guide *g, int *status, double *lastLoss, double *la
 
 /* ------------------------------------------------------------------ autotuner */
 
-/* Picks the BVH8 leaf size (1, 2, 3), the wavefront block size (64, 128, 256)
+/* Picks the BVH8's binary tree (the LBVH with leaves of up to 1 or 2
+ * triangles, or PLOC), the wavefront block size (64, 128, 256)
  * and the shading-queue compaction (per warp, per block) that render the
  * scene fastest (pixel-samples per second) at width x height with `spp`
  * samples timed after `warmupSpp` untimed ones (0 = 2), guiding mode

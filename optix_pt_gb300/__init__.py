@@ -253,12 +253,16 @@ class Renderer:
     """The reference's Renderer (include/renderer.h:19-206) on the GB300 engine."""
 
     def __init__(self, scene, spp_batch=0, block_size=0, leaf_size=0, use_graph=True, bvh_width=8, compaction=0,
-                 node_budget=0, tail_bounce=0):
+                 node_budget=0, tail_bounce=0, bvh_builder="lbvh"):
         """tail_bounce: first bounce finished by the path-completion kernel
-        (0 = the library's default, -1 = none: per-bounce kernels only)."""
+        (0 = the library's default, -1 = none: per-bounce kernels only).
+        bvh_builder: "lbvh" (default) or "ploc", the binary tree the 8-wide
+        BVH is collapsed from (the binary BVH is always the LBVH)."""
         self.scene = scene
+        if bvh_builder not in ("ploc", "lbvh"):
+            raise ValueError("bvh_builder must be 'ploc' or 'lbvh'")
         opt = _ffi.Options(spp_batch, block_size, leaf_size, 1 if use_graph else 0, bvh_width, compaction,
-                           node_budget, tail_bounce & 0xFFFFFFFF)
+                           node_budget, tail_bounce & 0xFFFFFFFF, 1 if bvh_builder == "ploc" else 0)
         h = ctypes.c_void_p()
         check(lib.optpt_create(ctypes.byref(scene.struct), ctypes.byref(opt), ctypes.byref(h)))
         self._h = h
@@ -695,7 +699,7 @@ def render_batch_scenes(renderers, views, stream=None):
 
 
 def autotune(scene, width, height, spp, warmup_spp=2, guiding=0):
-    """Times every (leaf size, block size, compaction) candidate on `scene`;
+    """Times every (tree, block size, compaction) candidate on `scene`;
     returns (best options as a dict, [trial dicts])."""
     req = _ffi.AutotuneRequest(width, height, spp, warmup_spp, guiding)
     best = _ffi.Options()

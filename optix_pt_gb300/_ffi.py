@@ -112,7 +112,7 @@ class SceneStruct(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("sppBatch", ctypes.c_uint32), ("blockSize", ctypes.c_uint32), ("leafSize", ctypes.c_uint32),
                 ("useGraph", ctypes.c_uint32), ("bvhWidth", ctypes.c_uint32), ("compaction", ctypes.c_uint32),
-                ("nodeBudget", ctypes.c_uint32), ("tailBounce", ctypes.c_uint32)]
+                ("nodeBudget", ctypes.c_uint32), ("tailBounce", ctypes.c_uint32), ("bvhBuilder", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):

@@ -1,7 +1,7 @@
 // Project-written autotuner for the wavefront tracer. It picks the launch
 // and build parameters the reference leaves to OptiX (src/renderer.cpp:
 // 441-513 builds the acceleration structure with OptiX's own choices): the
-// BVH8 leaf size, the wavefront block size and the shading-queue compaction
+// BVH8 tree (PLOC, or the LBVH with its leaf size), the wavefront block size and the shading-queue compaction
 // granularity, by timing each candidate on the caller's scene, then (plain
 // sampling) the bounce from which the path-completion kernel takes over,
 // with the chosen parameters. It is a client of the public C ABI (one
@@ -80,17 +80,20 @@ extern "C" int optpt_autotune(const optpt_scene *scene, const optpt_autotune_req
         return optpt_internal_set_error(OPTPT_ERR_INVALID, "NULL argument");
     if (req->width == 0 || req->height == 0 || req->spp == 0)
         return optpt_internal_set_error(OPTPT_ERR_INVALID, "autotune: width, height and spp must be positive");
-    static const uint32_t leaves[] = {1, 2, 3};
+    // the tree: the LBVH with leaves of up to one or two triangles, or PLOC
+    // (its leaves hold one triangle)
+    static const uint32_t trees[][2] = {{0, 1}, {0, 2}, {1, 1}};  // (bvhBuilder, leafSize)
     static const uint32_t blocks[] = {64, 128, 256};
     static const uint32_t compactions[] = {32, 1};
     double bestRate = -1.0;
     uint32_t n = 0;
     optpt_options chosen{};
-    for (uint32_t leaf : leaves)
+    for (const auto &tree : trees)
         for (uint32_t blk : blocks)
             for (uint32_t comp : compactions) {
                 optpt_options o{};
-                o.leafSize = leaf;
+                o.bvhBuilder = tree[0];
+                o.leafSize = tree[1];
                 o.blockSize = blk;
                 o.compaction = comp;
                 o.useGraph = 1;

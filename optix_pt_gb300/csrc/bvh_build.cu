@@ -12,6 +12,9 @@
 //   7. leaf-ordered triangle records (3 x float4) for traversal and shading
 // The arithmetic that decides codes and order uses explicitly rounded
 // operations so the host oracle reproduces codes, order and topology exactly.
+// Alternatively (an option for the 8-wide BVH) steps 4-6 are replaced by
+// PLOC clustering on the sorted triangles (below), which places large
+// triangles and sparse regions by surface area instead of by Morton bits.
 #include <cub/cub.cuh>
 #include "engine.h"
 
@@ -282,6 +285,119 @@ __global__ void kTriV(int n, const int *ids, const float *pos, const int *idx, c
     triV[3 * i + 2] = make_float4(c.x, c.y, c.z, __uint_as_float(flags ? flags[p] : 0u));
 }
 
+// ------------------------------------------------------------------ PLOC
+// Parallel locally-ordered clustering (Meister and Bittner, "Parallel
+// Locally-Ordered Clustering for Bounding Volume Hierarchy Construction",
+// IEEE TVCG 2018): the clusters (at first one per triangle, in Morton order)
+// each find the neighbour within PLOC_RADIUS positions whose merged box has
+// the smallest surface area; mutual neighbours merge into a new node, which
+// keeps the lower position; the survivors are compacted in order, and the
+// steps repeat until one cluster is left. Nodes are numbered downwards from
+// n - 2 in merge order, so the last merge (the root) is node 0. Ties are
+// broken by the pair's positions, so the smallest pair of every step is
+// mutual (progress) and the build is deterministic.
+#define PLOC_RADIUS 16
+#define PLOC_BLOCK 256
+
+OPT_D float mergedArea(float4 al, float4 ah, float4 bl, float4 bh)
+{
+    const float dx = fmaxf(ah.x, bh.x) - fminf(al.x, bl.x), dy = fmaxf(ah.y, bh.y) - fminf(al.y, bl.y),
+                dz = fmaxf(ah.z, bh.z) - fminf(al.z, bl.z);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// Cluster i = (lo.xyz, ref) / (hi.xyz, -); ref: node index, or sorted
+// triangle position | LEAF_BIT.
+__global__ void kPlocInit(int n, const int *ids, const float4 *plo, const float4 *phi, float4 *clo, float4 *chi)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const float4 l = plo[ids[i]], h = phi[ids[i]];
+    clo[i] = make_float4(l.x, l.y, l.z, __uint_as_float((unsigned)i | LEAF_BIT));
+    chi[i] = make_float4(h.x, h.y, h.z, 0.0f);
+}
+
+__global__ void __launch_bounds__(PLOC_BLOCK) kPlocNearest(int m, const float4 *clo, const float4 *chi, int *nn)
+{
+    __shared__ float4 sl[PLOC_BLOCK + 2 * PLOC_RADIUS], sh[PLOC_BLOCK + 2 * PLOC_RADIUS];
+    const int b0 = blockIdx.x * PLOC_BLOCK;
+    for (int k = threadIdx.x; k < PLOC_BLOCK + 2 * PLOC_RADIUS; k += PLOC_BLOCK) {
+        const int j = b0 - PLOC_RADIUS + k;
+        if (j >= 0 && j < m) {
+            sl[k] = clo[j];
+            sh[k] = chi[j];
+        }
+    }
+    __syncthreads();
+    const int i = b0 + threadIdx.x;
+    if (i >= m)
+        return;
+    const int si = threadIdx.x + PLOC_RADIUS;
+    const float4 al = sl[si], ah = sh[si];
+    float best = __int_as_float(0x7f800000);
+    int bj = -1;
+    for (int d = -PLOC_RADIUS; d <= PLOC_RADIUS; ++d) {
+        const int j = i + d;
+        if (d == 0 || j < 0 || j >= m)
+            continue;
+        const float a = mergedArea(al, ah, sl[si + d], sh[si + d]);
+        // ties: the pair with the lower (min, max) positions; for a fixed i
+        // that is the lower j
+        if (a < best || (a == best && j < bj)) {
+            best = a;
+            bj = j;
+        }
+    }
+    nn[i] = bj;
+}
+
+// keep[i] = cluster i survives this step (not the upper half of a merge);
+// merge[i] = cluster i merges with its upper neighbour.
+__global__ void kPlocFlags(int m, const int *nn, int *keep, int *merge)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    keep[i] = (mutual && j < i) ? 0 : 1;
+    merge[i] = (mutual && i < j) ? 1 : 0;
+}
+
+__global__ void kPlocEmit(int m, const float4 *clo, const float4 *chi, const int *nn, const int *keep,
+                          const int *keepPos, const int *merge, const int *mergePos, int nodeBase, BvhNode *nodes,
+                          float4 *olo, float4 *ohi)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !keep[i])
+        return;
+    const float4 al = clo[i], ah = chi[i];
+    const int pos = keepPos[i];
+    if (!merge[i]) {
+        olo[pos] = al;
+        ohi[pos] = ah;
+        return;
+    }
+    const int j = nn[i];
+    const float4 bl = clo[j], bh = chi[j];
+    const int node = nodeBase - 1 - mergePos[i];
+    int ref[2], cnt[2];
+    const unsigned r2[2] = {__float_as_uint(al.w), __float_as_uint(bl.w)};
+    for (int k = 0; k < 2; ++k) {
+        ref[k] = (int)(r2[k] & ~LEAF_BIT);
+        cnt[k] = (r2[k] & LEAF_BIT) ? 1 : 0;
+    }
+    BvhNode N;
+    N.a = make_float4(al.x, ah.x, al.y, ah.y);
+    N.b = make_float4(bl.x, bh.x, bl.y, bh.y);
+    N.c = make_float4(al.z, ah.z, bl.z, bh.z);
+    N.d = make_int4(ref[0], ref[1], cnt[0], cnt[1]);
+    nodes[node] = N;
+    olo[pos] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), __int_as_float(node));
+    ohi[pos] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.0f);
+}
+
 template <class T> cudaError_t dalloc(T *&p, size_t count)
 {
     return cudaMalloc((void **)&p, sizeof(T) * (count ? count : 1));
@@ -298,8 +414,89 @@ template <class T> cudaError_t dalloc(T *&p, size_t count)
         }                                                                                                              \
     } while (0)
 
+// The PLOC steps on sorted triangles: the BVH2 in out.nodes (n - 1 nodes,
+// leaves of one triangle). Synchronises `st` once per step for the counts.
+#define PLOC_MAX_STEPS 1024
+#define PLOC_GAVE_UP (-1)  // more steps than PLOC_MAX_STEPS: the caller builds the LBVH instead
+
+static int buildPloc(int n, const int *ids, const float4 *plo, const float4 *phi, BvhBuild &out, cudaStream_t st)
+{
+    cudaError_t err = cudaSuccess;
+    float4 *clo[2] = {nullptr, nullptr}, *chi[2] = {nullptr, nullptr};
+    int *nn = nullptr, *keep = nullptr, *merge = nullptr, *keepPos = nullptr, *mergePos = nullptr;
+    void *temp = nullptr;
+    size_t tempBytes = 0;
+    int m = n, nodeBase = n - 1, cur = 0, steps = 0;
+    const int B = 256;
+    CK(dalloc(clo[0], n));
+    CK(dalloc(clo[1], n));
+    CK(dalloc(chi[0], n));
+    CK(dalloc(chi[1], n));
+    CK(dalloc(nn, n));
+    CK(dalloc(keep, n));
+    CK(dalloc(merge, n));
+    CK(dalloc(keepPos, n));
+    CK(dalloc(mergePos, n));
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, tempBytes, keep, keepPos, n, st));
+    CK(cudaMalloc(&temp, tempBytes));
+    kPlocInit<<<(n + B - 1) / B, B, 0, st>>>(n, ids, plo, phi, clo[0], chi[0]);
+    CK(cudaGetLastError());
+    while (m > 1) {
+        if (++steps > PLOC_MAX_STEPS) {  // (a few dozen steps for ordinary scenes)
+            cudaFree(temp);
+            temp = nullptr;
+            err = cudaSuccess;
+            for (int k = 0; k < 2; ++k) {
+                cudaFree(clo[k]);
+                cudaFree(chi[k]);
+            }
+            cudaFree(nn);
+            cudaFree(keep);
+            cudaFree(merge);
+            cudaFree(keepPos);
+            cudaFree(mergePos);
+            return PLOC_GAVE_UP;
+        }
+        const int G = (m + B - 1) / B;
+        kPlocNearest<<<(m + PLOC_BLOCK - 1) / PLOC_BLOCK, PLOC_BLOCK, 0, st>>>(m, clo[cur], chi[cur], nn);
+        kPlocFlags<<<G, B, 0, st>>>(m, nn, keep, merge);
+        CK(cudaGetLastError());
+        CK(cub::DeviceScan::ExclusiveSum(temp, tempBytes, keep, keepPos, m, st));
+        CK(cub::DeviceScan::ExclusiveSum(temp, tempBytes, merge, mergePos, m, st));
+        kPlocEmit<<<G, B, 0, st>>>(m, clo[cur], chi[cur], nn, keep, keepPos, merge, mergePos, nodeBase, out.nodes,
+                                    clo[cur ^ 1], chi[cur ^ 1]);
+        CK(cudaGetLastError());
+        int last[4];
+        CK(cudaMemcpyAsync(last, keepPos + m - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(last + 1, keep + m - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(last + 2, mergePos + m - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(last + 3, merge + m - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        const int merges = last[2] + last[3];
+        if (merges <= 0) {  // cannot happen (the smallest pair is mutual); a broken step stops the build
+            err = cudaErrorUnknown;
+            goto done;
+        }
+        m = last[0] + last[1];
+        nodeBase -= merges;
+        cur ^= 1;
+    }
+done:
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(clo[k]);
+        cudaFree(chi[k]);
+    }
+    cudaFree(nn);
+    cudaFree(keep);
+    cudaFree(merge);
+    cudaFree(keepPos);
+    cudaFree(mergePos);
+    cudaFree(temp);
+    return (int)err;
+}
+
 int buildBvh(const float *positions, const int *triIndices, const int *matIndices, const uint32_t *triFlags,
-             int n, int leafSize, BvhBuild &out, cudaStream_t st)
+             int n, int leafSize, BvhBuild &out, cudaStream_t st, bool ploc)
 {
     out = BvhBuild{};
     if (n <= 0)
@@ -315,6 +512,7 @@ int buildBvh(const float *positions, const int *triIndices, const int *matIndice
     const unsigned cbInit[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
     const int nInt = n > 1 ? n - 1 : 1;
     const int B = 256, G = (n + B - 1) / B;
+    int pe = 0;
 
     CK(dalloc(plo, n));
     CK(dalloc(phi, n));
@@ -339,7 +537,14 @@ int buildBvh(const float *positions, const int *triIndices, const int *matIndice
 
     if (n == 1) {
         kSingle<<<1, 1, 0, st>>>(plo, phi, out.nodes, stats);
+    } else if (ploc && (pe = buildPloc(n, out.primOrder, plo, phi, out, st)) != PLOC_GAVE_UP) {
+        if (pe) {
+            err = (cudaError_t)pe;
+            goto done;
+        }
     } else {
+        ploc = false;
+        CK(cudaMemsetAsync(out.nodes, 0, sizeof(BvhNode) * nInt, st));
         CK(dalloc(child, n - 1));
         CK(dalloc(range, n - 1));
         CK(dalloc(parentI, n - 1));
@@ -359,8 +564,8 @@ int buildBvh(const float *positions, const int *triIndices, const int *matIndice
     CK(cudaMemcpyAsync(hstats, stats, sizeof(hstats), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     out.numNodes = nInt;
-    out.usedNodes = (int)hstats[0];
-    out.numLeaves = (int)hstats[1];
+    out.usedNodes = ploc && n > 1 ? n - 1 : (int)hstats[0];  // PLOC: every slot, leaves of one triangle
+    out.numLeaves = ploc && n > 1 ? n : (int)hstats[1];
 
 done:
     cudaFree(plo);

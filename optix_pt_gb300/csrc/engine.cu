@@ -892,8 +892,9 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
             rc = cudaFail(e, "scene upload");
             break;
         }
+        const bool ploc = r->opt.bvhWidth == 8 && r->opt.bvhBuilder == 1;
         int be = buildBvh(r->dPositions, r->dTriIndices, r->dMatIndices, r->dTriFlags, (int)nt, (int)r->opt.leafSize,
-                          r->bvh, r->ownStream);
+                          r->bvh, r->ownStream, ploc);
         if (be) {
             rc = cudaFail((cudaError_t)be, "BVH build");
             break;
@@ -901,6 +902,18 @@ int optpt_create(const optpt_scene *s, const optpt_options *options, optpt_rende
         if (r->opt.bvhWidth == 8 && (be = buildBvh8(r->bvh, (int)nt, r->ownStream))) {
             rc = cudaFail((cudaError_t)be, "BVH8 collapse");
             break;
+        }
+        if (ploc && r->bvh.nodes8 && r->bvh.levels8 > BVH8_STACK) {
+            // A PLOC tree too deep for the traversal stack (clusters at
+            // wildly different scales): the LBVH of the same order instead,
+            // whose depth the Morton bits bound.
+            freeBvh(r->bvh);
+            if ((be = buildBvh(r->dPositions, r->dTriIndices, r->dMatIndices, r->dTriFlags, (int)nt,
+                               (int)r->opt.leafSize, r->bvh, r->ownStream, false)) ||
+                (be = buildBvh8(r->bvh, (int)nt, r->ownStream))) {
+                rc = cudaFail((cudaError_t)be, "BVH build");
+                break;
+            }
         }
         // A ray's node-group stack holds at most one group per level below
         // the root: a tree of at most BVH8_STACK levels cannot overflow it.

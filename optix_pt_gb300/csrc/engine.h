@@ -247,10 +247,12 @@ struct BvhBuild {
 };
 // Collapses the BVH2 of `b` into b.nodes8 / b.triV8 (leaf sizes <= 4).
 int buildBvh8(BvhBuild &b, int numTris, cudaStream_t st);
-// Builds the LBVH on `st`. positions/triIndices/matIndices are device arrays;
-// triFlags (device, per primitive) go to triV[3i+2].w. Returns 0 or a CUDA error.
+// Builds the BVH2 on `st`: the LBVH, or with `ploc` the PLOC tree on the same
+// Morton order (leaves of one triangle; leafSize ignored). positions /
+// triIndices / matIndices are device arrays; triFlags (device, per primitive)
+// go to triV[3i+2].w. Returns 0 or a CUDA error.
 int buildBvh(const float *positions, const int *triIndices, const int *matIndices, const uint32_t *triFlags,
-             int numTris, int leafSize, BvhBuild &out, cudaStream_t st);
+             int numTris, int leafSize, BvhBuild &out, cudaStream_t st, bool ploc = false);
 void freeBvh(BvhBuild &b);
 // Refits the BVH8 in place after the vertex positions changed: triangle
 // records regathered, then every level's quantised child boxes recomputed

@@ -130,17 +130,18 @@ def test_autotune_measures_every_candidate(cuda_dev):
     best, trials = opt.autotune(sc, 96, 96, 16)
     grid, tails = trials[:18], trials[18:]
     assert len(trials) == 24
-    assert {(t["leafSize"], t["blockSize"], t["compaction"]) for t in grid} == {
-        (l, b, c) for l in (1, 2, 3) for b in (64, 128, 256) for c in (32, 1)}
+    assert {(t["bvhBuilder"], t["leafSize"], t["blockSize"], t["compaction"]) for t in grid} == {
+        (tb, tl, b, c) for tb, tl in ((0, 1), (0, 2), (1, 1)) for b in (64, 128, 256) for c in (32, 1)}
     # then the path-completion switch with the grid's best choices
     top = max(grid, key=lambda t: t["samples_per_s"])
     assert [t["tailBounce"] for t in tails] == [0xFFFFFFFF, 3, 4, 5, 6, 8]
-    assert all((t["leafSize"], t["blockSize"], t["compaction"]) == (top["leafSize"], top["blockSize"],
-                                                                     top["compaction"]) for t in tails)
+    assert all((t["bvhBuilder"], t["leafSize"], t["blockSize"], t["compaction"]) ==
+               (top["bvhBuilder"], top["leafSize"], top["blockSize"], top["compaction"]) for t in tails)
     assert all(t["samples_per_s"] > 0 and t["mrays_per_s"] > 0 for t in trials)
     fastest = max(trials, key=lambda t: t["samples_per_s"])
-    assert (best["leafSize"], best["blockSize"], best["compaction"], best["tailBounce"]) == (
-        fastest["leafSize"], fastest["blockSize"], fastest["compaction"], fastest["tailBounce"])
+    assert (best["bvhBuilder"], best["leafSize"], best["blockSize"], best["compaction"], best["tailBounce"]) == (
+        fastest["bvhBuilder"], fastest["leafSize"], fastest["blockSize"], fastest["compaction"],
+        fastest["tailBounce"])
     print("autotune best", best)
 
 

@@ -117,7 +117,7 @@ def test_bsdf_2pow24_queries_vs_fp64_oracle(cuda_dev):
 
 def _scene_from(arrays_scene, leaf=4, width=8):
     import optix_pt_gb300 as opt
-    return opt.Renderer(arrays_scene, leaf_size=leaf, bvh_width=width)
+    return opt.Renderer(arrays_scene, leaf_size=leaf, bvh_width=width, bvh_builder="lbvh")
 
 
 def _scenes():

@@ -238,6 +238,32 @@ def test_pipelined_launch_frames_match_synchronous_launch(cuda_dev):
     b.close()
 
 
+@pytest.mark.parametrize("name", ["spheres", "terrain_small"])
+def test_ploc_tree_renders_the_same_bits_as_the_lbvh(cuda_dev, name):
+    """The PLOC-derived BVH8 (one triangle per leaf, n - 1 nodes) gives the
+    same closest hits and occlusion as the LBVH's, so whole renders agree bit
+    for bit, ray counts included."""
+    import torch
+
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural(name)
+    out = []
+    for builder in ("lbvh", "ploc"):
+        r = opt.Renderer(sc, bvh_builder=builder)
+        r.setupOutputBuffer(160, 90)
+        r.render(4, torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        s, q, n = r.accum()
+        st = r.stats()
+        out.append((s, st))
+        if builder == "ploc":
+            assert st["bvhNodes"] == sc.num_triangles - 1 and st["bvhLeaves"] == sc.num_triangles
+        r.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    for k in ("extensionRays", "shadowRays", "pathSamples"):
+        assert out[0][1][k] == out[1][1][k], k
+
+
 def test_visualisation_albedo(cuda_dev):
     import optix_pt_gb300 as opt
     sc = opt.Scene.procedural("cornell")

@@ -54,7 +54,7 @@ def _rays(sc, n, seed):
 def test_bvh8_collapse_matches_host(cuda_dev, small, full, which, leaf):
     import optix_pt_gb300 as opt
     sc = small if which == "small" else full
-    r = opt.Renderer(sc, leaf_size=leaf, bvh_width=8)
+    r = opt.Renderer(sc, leaf_size=leaf, bvh_width=8, bvh_builder="lbvh")
     v = orc.SceneView(sc.struct, leaf)
     hn, ho = v.bvh8(sc.num_triangles)
     gn, go = r.bvh8_nodes()
@@ -64,11 +64,14 @@ def test_bvh8_collapse_matches_host(cuda_dev, small, full, which, leaf):
     r.close()
 
 
-@pytest.mark.parametrize("which,width", [("small", 8), ("small", 2), ("full", 8)])
-def test_closest_hits_bit_exact(cuda_dev, small, full, which, width):
+@pytest.mark.parametrize("which,width,builder", [("small", 8, "lbvh"), ("small", 2, "lbvh"), ("full", 8, "lbvh"),
+                                                   ("small", 8, "ploc"), ("full", 8, "ploc")])
+def test_closest_hits_bit_exact(cuda_dev, small, full, which, width, builder):
+    """Hits are a property of the ray and the scene: the same bits from the
+    LBVH- and PLOC-derived trees as from the host's own traversal."""
     import optix_pt_gb300 as opt
     sc = small if which == "small" else full
-    r = opt.Renderer(sc, leaf_size=3 if width == 8 else 4, bvh_width=width)
+    r = opt.Renderer(sc, leaf_size=3 if width == 8 else 4, bvh_width=width, bvh_builder=builder)
     v = orc.SceneView(sc.struct, 4)
     rays = _rays(sc, 1 << 17, 21)
     g = trace_on_gpu(r, rays, cuda_dev)

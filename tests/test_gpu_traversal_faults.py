@@ -92,8 +92,8 @@ def _rays_at_clusters(rng, centres, n):
     return np.concatenate([rays, rays_towards(rng, n // 4, (-50, 1100), (0, 1024))])
 
 
-@pytest.mark.parametrize("width", [8, 2])
-def test_deep_clustered_soup_needs_no_fault(cuda_dev, width):
+@pytest.mark.parametrize("width,builder", [(8, "lbvh"), (8, "ploc"), (2, "lbvh")])
+def test_deep_clustered_soup_needs_no_fault(cuda_dev, width, builder):
     import torch
 
     import optix_pt_gb300 as opt
@@ -101,7 +101,7 @@ def test_deep_clustered_soup_needs_no_fault(cuda_dev, width):
     v = orc.SceneView(sc.struct, 1)
     nodes = v.bvh(sc.num_triangles)[2]
     assert binary_depth(nodes) >= 40          # deep enough to matter for a 64-entry stack
-    r = opt.Renderer(sc, leaf_size=1, bvh_width=width)
+    r = opt.Renderer(sc, leaf_size=1, bvh_width=width, bvh_builder=builder)
     rng = np.random.default_rng(21)
     rays = _rays_at_clusters(rng, centres, 1 << 16)
     for any_hit in (False, True):
