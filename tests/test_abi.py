@@ -140,3 +140,15 @@ def test_calls_without_gpu_fail_cleanly(built):
     assert _ffi.lib.optpt_render(None, 1, None) == -1
     assert _ffi.lib.optpt_launch(None) == -1
     assert _ffi.lib.optpt_get_frame_buffer(None) is None or not _ffi.lib.optpt_get_frame_buffer(None)
+    # pipelined frame loop: a NULL renderer or output pointer is refused
+    frame = ctypes.POINTER(ctypes.c_float)()
+    assert _ffi.lib.optpt_launch_pipelined(None, ctypes.byref(frame)) == -1
+    assert _ffi.lib.optpt_launch_flush(None, ctypes.byref(frame)) == -1
+    assert _ffi.lib.optpt_guide_mixture_eval(None, 4, None, None, None) == -1
+
+
+def test_renderer_rejects_an_unknown_tree_builder(built):
+    import optix_pt_gb300 as opt
+    sc = opt.Scene.procedural("cornell")
+    with pytest.raises(ValueError):
+        opt.Renderer(sc, bvh_builder="sah")
