@@ -193,6 +193,20 @@ def _scene_for_oracle(name):
         os.remove(path)
 
 
+def reduce_over_ranks(values, n_max, world):
+    """The job's aggregate of per-rank measurements (a float64 tensor, the
+    same layout on every rank): the first n_max entries by their maximum over
+    ranks (times: the job is as slow as its slowest replica), the rest by
+    their sum (work: rays, samples). One rank: the values as they are."""
+    if world > 1:
+        import torch.distributed as dist
+        head, tail = values[:n_max].clone(), values[n_max:].clone()
+        dist.all_reduce(head, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tail, op=dist.ReduceOp.SUM)
+        return head.tolist() + tail.tolist()
+    return values.tolist()
+
+
 def _config(world):
     """The headline workload, as both arms report it (identical dicts)."""
     return dict(WORKLOAD, l2="flushed between timed steps (256 MB write, outside the events)")
@@ -351,13 +365,8 @@ def measure_frames(name, args, rank, world, dev, stream, with_cpu):
     del flush
     rays = (st1["extensionRays"] - st0["extensionRays"]) + (st1["shadowRays"] - st0["shadowRays"])
     samples = st1["pathSamples"] - st0["pathSamples"]
-    t = torch.tensor([ms, float(rays), float(samples)], dtype=torch.float64, device=dev)
-    if world > 1:
-        tmax = t.clone()
-        dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:3], op=dist.ReduceOp.SUM)
-        t[0] = tmax[0]
-    ms_all, rays_all, samples_all = t.tolist()
+    ms_all, rays_all, samples_all = reduce_over_ranks(
+        torch.tensor([ms, float(rays), float(samples)], dtype=torch.float64, device=dev), 1, world)
     value = rays_all / (ms_all / 1e3) / 1e6
 
     # End to end through the public API with host buffers: per step the frame
@@ -394,13 +403,9 @@ def measure_frames(name, args, rank, world, dev, stream, with_cpu):
         e2e_s = time.perf_counter() - t0
         st1 = r.stats()
         e2e_rays = (st1["extensionRays"] - st0["extensionRays"]) + (st1["shadowRays"] - st0["shadowRays"])
-        e = torch.tensor([e2e_s, float(e2e_rays)], dtype=torch.float64, device=dev)
-        if world > 1:
-            emax = e.clone()
-            dist.all_reduce(emax[0:1], op=dist.ReduceOp.MAX)
-            dist.all_reduce(e[1:2], op=dist.ReduceOp.SUM)
-            e[0] = emax[0]
-        return e[1].item() / e[0].item() / 1e6
+        e_s, e_rays = reduce_over_ranks(torch.tensor([e2e_s, float(e2e_rays)], dtype=torch.float64, device=dev),
+                                        1, world)
+        return e_rays / e_s / 1e6
 
     e2e_sync = e2e_run(False)
     e2e_value = e2e_run(True)
